@@ -1,0 +1,200 @@
+// Tile FFT building blocks for the MS-OSM engine (sm_103a).
+//
+// A CTA transforms COLS independent length-N sequences ("columns") held in
+// shared memory.  Stages are Stockham autosort stages of radix 8 (then 4 or 2
+// to finish), each thread owning BPT butterflies per stage with all R inputs in
+// registers.  The first stage may read straight from global memory through a
+// loader functor and the last stage may hand its outputs to an epilogue functor
+// instead of shared memory, so a pass touches shared memory only between stages.
+//
+// Shared layout: element (col, n) lives at n*LD + col with LD = COLS + 1.  A
+// warp always covers 16 consecutive columns of one or two rows, so with the pad
+// every access is the minimal two wavefronts for 256 bytes.
+//
+// Stage (R, Ns):  butterfly j (0 <= j < N/R), k = j mod Ns
+//   in  : x[j + r*N/R] * W_{Ns*R}^{r*k}          (r = 0..R-1)
+//   out : y[(j/Ns)*Ns*R + k + r*Ns] = DFT_R(in)[r]
+// W_N^m = exp(SIGN * 2*pi*i*m/N); SIGN = -1 forward, +1 inverse (unnormalised),
+// the cuFFT convention the reference's transforms use.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace msosm {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * (SIGN * i)
+template <int SIGN>
+__device__ __forceinline__ float2 cmul_si(float2 a)
+{
+    return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft2(float2 *v)
+{
+    float2 t = csub(v[0], v[1]);
+    v[0] = cadd(v[0], v[1]);
+    v[1] = t;
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3)
+{
+    float2 a = cadd(v0, v2), b = csub(v0, v2);
+    float2 c = cadd(v1, v3), d = cmul_si<SIGN>(csub(v1, v3));
+    v0 = cadd(a, c);
+    v2 = csub(a, c);
+    v1 = cadd(b, d);
+    v3 = csub(b, d);
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2 *v)
+{
+    dft4<SIGN>(v[0], v[1], v[2], v[3]);
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft8(float2 *v)
+{
+    const float c = 0.70710678118654752440f;
+    float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<SIGN>(e0, e1, e2, e3);
+    dft4<SIGN>(o0, o1, o2, o3);
+    // W8^1 * o1 = c*(o.x - s*o.y, s*o.x + o.y); W8^2 = s*i; W8^3 * o = c*(-o.x - s*o.y, s*o.x - o.y)
+    const float s = (float)SIGN;
+    float2 t1 = make_float2(c * (o1.x - s * o1.y), c * (s * o1.x + o1.y));
+    float2 t2 = cmul_si<SIGN>(o2);
+    float2 t3 = make_float2(c * (-o3.x - s * o3.y), c * (s * o3.x - o3.y));
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, t1);
+    v[5] = csub(e1, t1);
+    v[2] = cadd(e2, t2);
+    v[6] = csub(e2, t2);
+    v[3] = cadd(e3, t3);
+    v[7] = csub(e3, t3);
+}
+
+template <int R, int SIGN>
+__device__ __forceinline__ void dftR(float2 *v)
+{
+    if constexpr (R == 8)
+        dft8<SIGN>(v);
+    else if constexpr (R == 4)
+        dft4<SIGN>(v);
+    else
+        dft2<SIGN>(v);
+}
+
+// Radix of the stage that starts with sub-transform size Ns.
+template <int N, int Ns>
+struct StageRadix
+{
+    static constexpr int value = (N / Ns >= 8) ? 8 : (N / Ns);
+};
+
+template <int N, int COLS>
+struct TileGeom
+{
+    static constexpr int LD = COLS + 1;
+    static constexpr int SMEM_ELEMS = N * LD;
+};
+
+// Shared-memory source/destination for a stage.
+template <int N, int COLS>
+struct SmemIO
+{
+    float2 *sm;
+    __device__ __forceinline__ float2 load(int col, int n) const { return sm[n * TileGeom<N, COLS>::LD + col]; }
+    __device__ __forceinline__ void store(int col, int n, float2 v) const { sm[n * TileGeom<N, COLS>::LD + col] = v; }
+};
+
+// One Stockham stage.  SRC/DST provide load(col, n) / store(col, n, v).
+// SRC_SMEM / DST_SMEM say whether they alias the CTA's shared tile, which decides
+// the barriers.  tw: W_N^m table (SIGN applied), N entries, shared memory.
+template <int N, int COLS, int THREADS, int SIGN, int Ns, bool SRC_SMEM, bool DST_SMEM, class SRC, class DST>
+__device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const float2 *__restrict__ tw)
+{
+    constexpr int R = StageRadix<N, Ns>::value;
+    constexpr int NB = COLS * N / R;
+    static_assert(NB % THREADS == 0, "butterflies must divide evenly over threads");
+    constexpr int BPT = NB / THREADS;
+    constexpr int STRIDE = N / R;
+    constexpr int TWSTEP = N / (Ns * R);
+    float2 v[BPT][R];
+#pragma unroll
+    for (int i = 0; i < BPT; i++)
+    {
+        const int beta = threadIdx.x + i * THREADS;
+        const int col = beta % COLS;
+        const int j = beta / COLS;
+        const int k = j & (Ns - 1);
+#pragma unroll
+        for (int r = 0; r < R; r++)
+        {
+            float2 a = src.load(col, j + r * STRIDE);
+            if constexpr (Ns > 1)
+            {
+                if (r > 0)
+                    a = cmul(a, tw[r * k * TWSTEP]);
+            }
+            v[i][r] = a;
+        }
+    }
+    if constexpr (SRC_SMEM && DST_SMEM)
+        __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; i++)
+    {
+        dftR<R, SIGN>(v[i]);
+        const int beta = threadIdx.x + i * THREADS;
+        const int col = beta % COLS;
+        const int j = beta / COLS;
+        const int k = j & (Ns - 1);
+        const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            dst.store(col, base + r * Ns, v[i][r]);
+    }
+    if constexpr (DST_SMEM)
+        __syncthreads();
+}
+
+// Run all stages from Ns onwards.  FIRST: the stage at Ns reads from `first`
+// (global loader) instead of shared memory.  The final stage hands its outputs to
+// `last` (epilogue) instead of shared memory.
+template <int N, int COLS, int THREADS, int SIGN, int Ns, bool FIRST_FROM_LOADER, class LOADER, class EPI>
+__device__ __forceinline__ void fft_stages(float2 *sm, const float2 *tw, const LOADER &first, const EPI &last)
+{
+    constexpr int R = StageRadix<N, Ns>::value;
+    constexpr bool IS_LAST = (Ns * R == N);
+    SmemIO<N, COLS> io{sm};
+    if constexpr (FIRST_FROM_LOADER && IS_LAST)
+        fft_stage<N, COLS, THREADS, SIGN, Ns, false, false>(first, last, tw);
+    else if constexpr (FIRST_FROM_LOADER)
+        fft_stage<N, COLS, THREADS, SIGN, Ns, false, true>(first, io, tw);
+    else if constexpr (IS_LAST)
+        fft_stage<N, COLS, THREADS, SIGN, Ns, true, false>(io, last, tw);
+    else
+        fft_stage<N, COLS, THREADS, SIGN, Ns, true, true>(io, io, tw);
+    if constexpr (!IS_LAST)
+        fft_stages<N, COLS, THREADS, SIGN, Ns * R, false>(sm, tw, first, last);
+}
+
+// Twiddle table W_N^m (m < N) into shared memory from a global table of W_N.
+template <int N, int THREADS>
+__device__ __forceinline__ void load_twiddles(float2 *tw_sm, const float2 *__restrict__ tw_g)
+{
+    for (int i = threadIdx.x; i < N; i += THREADS)
+        tw_sm[i] = __ldg(tw_g + i);
+}
+
+} // namespace msosm

@@ -1,0 +1,943 @@
+// C ABI of the MS-OSM engine (declared in include/msosm_gb300.h).
+//
+// Host orchestration of one streaming step, mirroring
+// MSOSM_GPU_BATCH::filter_block_uint16 (dedispersion/msosm/msosm_gpu_batch.cpp:178-236):
+//   1. new samples reach the device (copied when `in` is host memory, read in
+//      place when it is device memory);
+//   2. forward transforms of the B overlapping windows into ring slots
+//      rbi..rbi+B-1, rbi = (step*B) mod fbs (increment_fft_output, :167-176); the
+//      decode and the tail hand-over (increment_fft_input, :153-165) are fused in;
+//   3. for every (DM, window), in chunks sized for L2: gather x response ->
+//      inverse -> discard/scale -> outputs and/or fold.
+// Everything is ordered on the caller's stream; nothing synchronises the device.
+#include "msosm_gb300.h"
+
+#include "msosm_kernels.cuh"
+#include "msosm_plan.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+using msosm::Geom;
+using msosm::Twiddles;
+
+namespace {
+
+constexpr int kMinLog2F = 8;
+constexpr int kMaxLog2F = 22;
+constexpr size_t kIntermediateBudget = 64ull << 20; // bytes of pass-1 output kept per launch pair
+constexpr unsigned kMaxFusedBins = 8192;
+
+size_t in_elem_bytes(int fmt)
+{
+    switch (fmt)
+    {
+    case MSOSM_IN_U16: return 4;
+    case MSOSM_IN_C64: return 8;
+    case MSOSM_IN_I8: return 2;
+    default: return 0;
+    }
+}
+
+bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+int ilog2(long long v)
+{
+    int l = 0;
+    while ((1ll << l) < v)
+        l++;
+    return l;
+}
+
+// Fraction of a turn in Q0.64 fixed point.
+uint64_t turns_q64(long double turns)
+{
+    long double f = turns - floorl(turns);
+    long double v = ldexpl(f, 64);
+    if (!(v < 18446744073709551616.0L))
+        return 0;
+    if (v < 0)
+        return 0;
+    return (uint64_t)v;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0)
+        return cudaSuccess;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+void dfree(void *p)
+{
+    if (p)
+        cudaFree(p);
+}
+
+// Kernel timing: with timing on, each launch is bracketed by a pair of CUDA
+// events recorded on its stream; elapsed times are summed when read (after a
+// stream sync), so timing never blocks the launch path.  Launches and
+// transforms are counted whether or not timing is on.
+struct Profiler
+{
+    static constexpr int KINDS = 4;
+    bool on = false;
+    long long launches[KINDS] = {0, 0, 0, 0};
+    long long transforms[KINDS] = {0, 0, 0, 0};
+    double ms[KINDS] = {0, 0, 0, 0};
+    long long timed[KINDS] = {0, 0, 0, 0};
+    struct Pending
+    {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t cur = nullptr;
+
+    cudaEvent_t get()
+    {
+        if (!pool.empty())
+        {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return e;
+    }
+    void begin(int, cudaStream_t st)
+    {
+        if (!on)
+            return;
+        cur = get();
+        if (cur)
+            cudaEventRecord(cur, st);
+    }
+    void end(int kind, cudaStream_t st, long long ntrans)
+    {
+        launches[kind]++;
+        transforms[kind] += ntrans;
+        if (!on || !cur)
+            return;
+        cudaEvent_t b = get();
+        if (!b)
+            return;
+        cudaEventRecord(b, st);
+        pending.push_back({kind, cur, b});
+        cur = nullptr;
+    }
+    // Resolve recorded pairs; call after the stream(s) completed.
+    cudaError_t collect()
+    {
+        for (auto &p : pending)
+        {
+            float t = 0.f;
+            cudaError_t e = cudaEventElapsedTime(&t, p.a, p.b);
+            if (e != cudaSuccess)
+                return e;
+            ms[p.kind] += t;
+            timed[p.kind]++;
+            pool.push_back(p.a);
+            pool.push_back(p.b);
+        }
+        pending.clear();
+        return cudaSuccess;
+    }
+    void reset()
+    {
+        collect();
+        for (int k = 0; k < KINDS; k++)
+        {
+            launches[k] = transforms[k] = timed[k] = 0;
+            ms[k] = 0;
+        }
+    }
+    ~Profiler()
+    {
+        for (auto &p : pending)
+        {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        for (auto e : pool)
+            cudaEventDestroy(e);
+    }
+};
+
+} // namespace
+
+struct msosm_fold_s
+{
+    float period = 0, fs = 0;
+    double P = 0, dt = 0, t_start = 0;
+    unsigned long size = 0, K = 0;
+    int S = 0;
+    double *d_sum = nullptr;
+    unsigned long long *d_cnt = nullptr;
+    float *d_folded = nullptr;
+    std::string err;
+
+    msosm::FoldArgs args() const
+    {
+        msosm::FoldArgs a;
+        a.sum = d_sum;
+        a.cnt = d_cnt;
+        a.phase0 = turns_q64((long double)t_start / (long double)P);
+        a.dphase = turns_q64((long double)dt / (long double)P);
+        a.K = (unsigned)K;
+        return a;
+    }
+    ~msosm_fold_s()
+    {
+        dfree(d_sum);
+        dfree(d_cnt);
+        dfree(d_folded);
+    }
+};
+
+struct msosm_s
+{
+    bool osm = false;
+    float bw = 0, f0 = 0;
+    std::vector<float> dms;
+    int D = 0;
+    std::vector<int> nd, dc;
+    int M_min = 0, M = 0, F = 0, B = 0, fbs = 0, delaycount = 0;
+    int in_format = 0, out_mode = 0;
+    bool inited = false;
+    Geom g{};
+    // device state
+    float2 *d_ring = nullptr;
+    float2 *d_H = nullptr;
+    uint16_t *d_delays = nullptr;
+    float2 *d_T = nullptr;
+    int T_cap = 0;
+    float2 *d_tail[2] = {nullptr, nullptr};
+    int tail_cur = 0;
+    void *d_in = nullptr;
+    float2 *d_out_c64 = nullptr;
+    uint32_t *d_out_u16 = nullptr;
+    float2 *d_tw = nullptr;
+    Twiddles tw_fwd{}, tw_inv{};
+    long long step = 0;
+    msosm_fold_t *fold = nullptr;
+    Profiler prof;
+    std::string err;
+
+    int fail(int code, const std::string &msg)
+    {
+        err = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what)
+    {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return MSOSM_ERR_CUDA;
+    }
+    void release()
+    {
+        dfree(d_ring);
+        dfree(d_H);
+        dfree(d_delays);
+        dfree(d_T);
+        dfree(d_tail[0]);
+        dfree(d_tail[1]);
+        dfree(d_in);
+        dfree(d_out_c64);
+        dfree(d_out_u16);
+        dfree(d_tw);
+        d_ring = d_H = d_T = d_out_c64 = d_tw = nullptr;
+        d_tail[0] = d_tail[1] = nullptr;
+        d_delays = nullptr;
+        d_in = nullptr;
+        d_out_u16 = nullptr;
+        inited = false;
+    }
+    ~msosm_s() { release(); }
+};
+
+// -----------------------------------------------------------------------------
+extern "C" const char *msosm_version(void) { return "msosm_gb300 0.1 (sm_103a)"; }
+
+extern "C" const char *msosm_status_string(int s)
+{
+    switch (s)
+    {
+    case MSOSM_OK: return "ok";
+    case MSOSM_ERR_ARG: return "invalid argument";
+    case MSOSM_ERR_STATE: return "call out of order";
+    case MSOSM_ERR_CUDA: return "CUDA error";
+    case MSOSM_ERR_NOMEM: return "out of memory";
+    case MSOSM_ERR_UNSUPPORTED: return "unsupported configuration";
+    default: return "unknown status";
+    }
+}
+
+// ---- host-only planning ------------------------------------------------------
+extern "C" int msosm_plan_nd(float bw, float f0, const float *dms, int num_dms, int *nd_out)
+{
+    if (!dms || !nd_out || num_dms <= 0)
+        return MSOSM_ERR_ARG;
+    for (int i = 0; i < num_dms; i++)
+        nd_out[i] = msosm::plan_nd(bw, dms[i], f0);
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_plan_min_order(const int *nd, int num_dms, int *M_min_out)
+{
+    if (!nd || !M_min_out || num_dms <= 0)
+        return MSOSM_ERR_ARG;
+    int m = 0;
+    for (int i = 0; i < num_dms; i++)
+        m = std::max(m, msosm::plan_min_order(nd[i]));
+    *M_min_out = m;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_plan_segmentation(float bw, float f0, float dm, int nd, int M, int *delay_out, int *dc_out)
+{
+    if (M <= 0 || !delay_out)
+        return MSOSM_ERR_ARG;
+    if (msosm::plan_delaycount(nd, M) > 65535)
+        return MSOSM_ERR_UNSUPPORTED;
+    std::vector<uint16_t> d((size_t)2 * M);
+    const int dc = msosm::plan_segmentation(bw, f0, dm, nd, M, d.data());
+    for (size_t i = 0; i < d.size(); i++)
+        delay_out[i] = d[i];
+    if (dc_out)
+        *dc_out = dc;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_plan_response(float bw, float f0, float dm, int M, float *H_out)
+{
+    if (M <= 0 || !is_pow2(M) || !H_out)
+        return MSOSM_ERR_ARG;
+    msosm::plan_response(bw, f0, dm, M, H_out);
+    return MSOSM_OK;
+}
+
+extern "C" int osm_plan(float bw, float dm, float f0, unsigned long *nd_out, unsigned long *M_min_out)
+{
+    const unsigned long nd = msosm::plan_osm_nd(bw, dm, f0);
+    if (nd_out)
+        *nd_out = nd;
+    if (M_min_out)
+        *M_min_out = msosm::plan_osm_min_order(nd);
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_create(float bw, float f0, const float *dms, int num_dms, msosm_t **out)
+{
+    if (!out)
+        return MSOSM_ERR_ARG;
+    *out = nullptr;
+    if (num_dms <= 0 || !dms || !(bw > 0) || !(f0 > 0))
+        return MSOSM_ERR_ARG;
+    for (int i = 0; i < num_dms; i++)
+        if (!(dms[i] >= 0) || (i > 0 && dms[i] < dms[i - 1]))
+            return MSOSM_ERR_ARG; // DMs must be non-negative and ascending
+    msosm_t *h = new (std::nothrow) msosm_s();
+    if (!h)
+        return MSOSM_ERR_NOMEM;
+    h->bw = bw;
+    h->f0 = f0;
+    h->dms.assign(dms, dms + num_dms);
+    h->D = num_dms;
+    h->nd.resize(num_dms);
+    h->M_min = 0;
+    for (int i = 0; i < num_dms; i++)
+    {
+        h->nd[i] = msosm::plan_nd(bw, dms[i], f0);
+        h->M_min = std::max(h->M_min, msosm::plan_min_order(h->nd[i]));
+    }
+    *out = h;
+    return MSOSM_OK;
+}
+
+extern "C" int osm_create(float bw, float dm, float f0, msosm_t **out)
+{
+    if (!out)
+        return MSOSM_ERR_ARG;
+    *out = nullptr;
+    if (!(bw > 0) || !(f0 > 0) || !(dm >= 0))
+        return MSOSM_ERR_ARG;
+    msosm_t *h = new (std::nothrow) msosm_s();
+    if (!h)
+        return MSOSM_ERR_NOMEM;
+    h->osm = true;
+    h->bw = bw;
+    h->f0 = f0;
+    h->dms.assign(1, dm);
+    h->D = 1;
+    const unsigned long nd = msosm::plan_osm_nd(bw, dm, f0);
+    h->nd.assign(1, (int)nd);
+    const unsigned long mmin = msosm::plan_osm_min_order(nd);
+    h->M_min = (int)std::min<unsigned long>(mmin, 1ul << 30);
+    *out = h;
+    return MSOSM_OK;
+}
+
+static int build_twiddles(msosm_t *h)
+{
+    const int N1 = h->g.N1, N2 = h->g.N2, F = h->g.F;
+    // per direction: twN1 (N1), twN2 (N2), lo (N2), hi (N1)
+    const size_t per = (size_t)2 * N1 + 2 * N2;
+    std::vector<float2> host(2 * per);
+    const double PI = 3.14159265358979323846;
+    for (int dir = 0; dir < 2; dir++)
+    {
+        const double sgn = dir == 0 ? -1.0 : 1.0;
+        float2 *base = host.data() + dir * per;
+        auto w = [&](long long m, long long n) {
+            // exp(sgn*2*pi*i*m/n) with m reduced exactly
+            const double a = 2.0 * PI * (double)(m % n) / (double)n;
+            return make_float2((float)std::cos(a), (float)(sgn * std::sin(a)));
+        };
+        for (int m = 0; m < N1; m++)
+            base[m] = w(m, N1);
+        for (int m = 0; m < N2; m++)
+            base[N1 + m] = w(m, N2);
+        for (int m = 0; m < N2; m++)
+            base[N1 + N2 + m] = w(m, F);
+        for (int m = 0; m < N1; m++)
+            base[N1 + 2 * N2 + m] = w((long long)m * N2, F);
+    }
+    cudaError_t e = dalloc(&h->d_tw, host.size());
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "cudaMalloc(twiddles)");
+    e = cudaMemcpy(h->d_tw, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "cudaMemcpy(twiddles)");
+    for (int dir = 0; dir < 2; dir++)
+    {
+        float2 *base = h->d_tw + dir * per;
+        Twiddles t{base, base + N1, base + N1 + N2, base + N1 + 2 * N2};
+        (dir == 0 ? h->tw_fwd : h->tw_inv) = t;
+    }
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, int out_mode)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (h->inited)
+        return h->fail(MSOSM_ERR_STATE, "msosm_init called twice");
+    if (batch <= 0)
+        return h->fail(MSOSM_ERR_ARG, "batch must be positive");
+    if (in_elem_bytes(in_format) == 0)
+        return h->fail(MSOSM_ERR_ARG, "unknown input format");
+    if (out_mode & ~(MSOSM_OUT_C64 | MSOSM_OUT_U16))
+        return h->fail(MSOSM_ERR_ARG, "unknown output mode bits");
+    if (fftpoint < 0)
+        return h->fail(MSOSM_ERR_ARG, "fftpoint must be >= 0");
+    // initialize_uint16's rule (msosm_gpu_batch.cpp:32-41 / osm_gpu_batch.cpp:27-37)
+    int M = h->M_min;
+    if (fftpoint != 0)
+    {
+        M = fftpoint / 2;
+        if (M < h->M_min)
+        {
+            std::fprintf(stderr,
+                         "Warning: The filter order is too small for the given FFT point. The minimum FFT point %d "
+                         "is used.\n",
+                         2 * h->M_min);
+            M = h->M_min;
+        }
+    }
+    const long long F = 2ll * M;
+    if (!is_pow2(F) || ilog2(F) < kMinLog2F || ilog2(F) > kMaxLog2F)
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "FFT size " + std::to_string(F) + " outside [2^8, 2^22]");
+    h->M = M;
+    h->F = (int)F;
+    h->B = batch;
+    h->in_format = in_format;
+    h->out_mode = out_mode;
+    const int L = ilog2(F);
+    h->g = Geom{L, (int)F, M, 1 << (L / 2), 1 << (L - L / 2)};
+
+    // segmentation of every DM (msosm_gpu_batch.cpp:150-157)
+    const size_t DF = (size_t)h->D * F;
+    std::vector<uint16_t> delays(DF, 0);
+    h->dc.assign(h->D, 0);
+    h->delaycount = 0;
+    if (!h->osm)
+    {
+        for (int i = 0; i < h->D; i++)
+        {
+            const int dc = msosm::plan_delaycount(h->nd[i], M);
+            if (dc > 65535)
+                return h->fail(MSOSM_ERR_UNSUPPORTED, "delaycount above 65535");
+            h->dc[i] = msosm::plan_segmentation(h->bw, h->f0, h->dms[i], h->nd[i], M, delays.data() + (size_t)i * F);
+            h->delaycount = std::max(h->delaycount, h->dc[i]);
+        }
+    }
+    else
+    {
+        h->dc[0] = 1;
+        h->delaycount = 1;
+    }
+    // ring of past spectra (msosm_gpu_batch.cpp:113-122), at least one batch
+    int fbs = h->delaycount + batch - 1;
+    if (fbs % batch)
+        fbs += batch - fbs % batch;
+    h->fbs = std::max(fbs, batch);
+
+    // responses (msosm_gpu_batch.cpp:183-189) on host threads, FP64 inside
+    std::vector<float> H(2 * DF);
+    const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    msosm::plan_responses(h->bw, h->f0, h->dms.data(), h->D, M, H.data(), threads);
+
+    cudaError_t e;
+    const size_t ring_elems = (size_t)h->fbs * F;
+    if ((e = dalloc(&h->d_ring, ring_elems)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMalloc(ring)");
+    if ((e = cudaMemset(h->d_ring, 0, ring_elems * sizeof(float2))) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMemset(ring)");
+    if ((e = dalloc(&h->d_H, DF)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMalloc(H)");
+    if ((e = cudaMemcpy(h->d_H, H.data(), DF * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMemcpy(H)");
+    if ((e = dalloc(&h->d_delays, DF)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMalloc(delays)");
+    if ((e = cudaMemcpy(h->d_delays, delays.data(), DF * sizeof(uint16_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMemcpy(delays)");
+    const long long per_launch = (long long)(kIntermediateBudget / ((size_t)F * sizeof(float2)));
+    h->T_cap = (int)std::max<long long>(batch, std::min<long long>((long long)h->D * batch, std::max(1ll, per_launch)));
+    if ((e = dalloc(&h->d_T, (size_t)h->T_cap * F)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMalloc(intermediate)");
+    for (int i = 0; i < 2; i++)
+    {
+        if ((e = dalloc(&h->d_tail[i], (size_t)M)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMalloc(tail)");
+        if ((e = cudaMemset(h->d_tail[i], 0, (size_t)M * sizeof(float2))) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMemset(tail)");
+    }
+    const size_t in_bytes = (size_t)batch * M * in_elem_bytes(in_format);
+    if ((e = cudaMalloc(&h->d_in, in_bytes)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaMalloc(input)");
+    const size_t out_elems = (size_t)h->D * batch * M;
+    if (out_mode & MSOSM_OUT_C64)
+        if ((e = dalloc(&h->d_out_c64, out_elems)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMalloc(output)");
+    if (out_mode & MSOSM_OUT_U16)
+        if ((e = dalloc(&h->d_out_u16, out_elems)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMalloc(output u16)");
+    int rc = build_twiddles(h);
+    if (rc != MSOSM_OK)
+        return h->release(), rc;
+    h->step = 0;
+    h->tail_cur = 0;
+    h->inited = true;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_dims(const msosm_t *h, int *M, int *M_min, int *fftpoint, int *batch, int *num_dms,
+                              int *delaycount, int *ring_blocks)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (M)
+        *M = h->M;
+    if (M_min)
+        *M_min = h->M_min;
+    if (fftpoint)
+        *fftpoint = h->F;
+    if (batch)
+        *batch = h->B;
+    if (num_dms)
+        *num_dms = h->D;
+    if (delaycount)
+        *delaycount = h->delaycount;
+    if (ring_blocks)
+        *ring_blocks = h->fbs;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_nd(const msosm_t *h, int *nd_out)
+{
+    if (!h || !nd_out)
+        return MSOSM_ERR_ARG;
+    std::copy(h->nd.begin(), h->nd.end(), nd_out);
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_delaycounts(const msosm_t *h, int *dc_out)
+{
+    if (!h || !dc_out)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return MSOSM_ERR_STATE;
+    std::copy(h->dc.begin(), h->dc.end(), dc_out);
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_delay_points(const msosm_t *h, int dm_index, int *out)
+{
+    if (!h || !out || dm_index < 0 || dm_index >= h->D)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return MSOSM_ERR_STATE;
+    std::vector<uint16_t> tmp(h->F);
+    cudaError_t e = cudaMemcpy(tmp.data(), h->d_delays + (size_t)dm_index * h->F, h->F * sizeof(uint16_t),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return const_cast<msosm_t *>(h)->cuda_fail(e, "cudaMemcpy(delays)");
+    for (int i = 0; i < h->F; i++)
+        out[i] = tmp[i];
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_response(const msosm_t *h, int dm_index, float *out)
+{
+    if (!h || !out || dm_index < 0 || dm_index >= h->D)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return MSOSM_ERR_STATE;
+    cudaError_t e =
+        cudaMemcpy(out, h->d_H + (size_t)dm_index * h->F, (size_t)h->F * sizeof(float2), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return const_cast<msosm_t *>(h)->cuda_fail(e, "cudaMemcpy(H)");
+    return MSOSM_OK;
+}
+
+static bool is_device_pointer(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream_t st)
+{
+    const size_t in_bytes = (size_t)h->B * h->M * in_elem_bytes(h->in_format);
+    const void *src = in;
+    cudaError_t e;
+    if (!in_on_device)
+    {
+        if ((e = cudaMemcpyAsync(h->d_in, in, in_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return h->cuda_fail(e, "cudaMemcpyAsync(input)");
+        src = h->d_in;
+    }
+    const int rbi = (int)((h->step * h->B) % h->fbs);
+    const float2 *tail = h->d_tail[h->tail_cur];
+    float2 *tail_next = h->d_tail[h->tail_cur ^ 1];
+    Profiler &pr = h->prof;
+    pr.begin(MSOSM_KERNEL_FWD_PASS1, st);
+    e = msosm::launch_forward_p1(h->g, h->tw_fwd, h->in_format, src, tail, tail_next, h->d_T, h->B, st);
+    pr.end(MSOSM_KERNEL_FWD_PASS1, st, h->B);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "forward transform launch (pass 1)");
+    pr.begin(MSOSM_KERNEL_FWD_PASS2, st);
+    e = msosm::launch_forward_p2(h->g, h->tw_fwd, h->d_T, h->d_ring, rbi, h->B, st);
+    pr.end(MSOSM_KERNEL_FWD_PASS2, st, h->B);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "forward transform launch (pass 2)");
+
+    msosm::InvArgs a{};
+    a.ring = h->d_ring;
+    a.H = h->d_H;
+    a.delays = h->d_delays;
+    a.T = h->d_T;
+    a.rbi = rbi;
+    a.fbs = h->fbs;
+    a.B = h->B;
+    a.out_mode = 0;
+    if (h->out_mode & MSOSM_OUT_C64)
+        a.out_mode |= msosm::OUT_C64;
+    if (h->out_mode & MSOSM_OUT_U16)
+        a.out_mode |= msosm::OUT_U16;
+    a.out_c64 = h->d_out_c64;
+    a.out_u16 = h->d_out_u16;
+    if (h->fold)
+    {
+        a.out_mode |= msosm::OUT_FOLD;
+        a.fold = h->fold->args();
+    }
+    const long long total = (long long)h->D * h->B;
+    for (long long g0 = 0; g0 < total; g0 += h->T_cap)
+    {
+        const int count = (int)std::min<long long>(h->T_cap, total - g0);
+        pr.begin(MSOSM_KERNEL_INV_PASS1, st);
+        e = msosm::launch_inverse_p1(h->g, h->tw_inv, a, g0, count, st);
+        pr.end(MSOSM_KERNEL_INV_PASS1, st, count);
+        if (e != cudaSuccess)
+            return h->cuda_fail(e, "inverse transform launch (pass 1)");
+        pr.begin(MSOSM_KERNEL_INV_PASS2, st);
+        e = msosm::launch_inverse_p2(h->g, h->tw_inv, a, g0, count, st);
+        pr.end(MSOSM_KERNEL_INV_PASS2, st, count);
+        if (e != cudaSuccess)
+            return h->cuda_fail(e, "inverse transform launch (pass 2)");
+    }
+    if (h->fold)
+        h->fold->t_start += (double)((size_t)h->B * h->M) * h->fold->dt; // fold_gpu.cpp:96
+    h->tail_cur ^= 1;
+    h->step++;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_process(msosm_t *h, const void *in, void *stream)
+{
+    return msosm_process_many(h, in, 1, stream);
+}
+
+extern "C" int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *stream)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "msosm_process before msosm_init");
+    if (!in || nsteps < 0)
+        return h->fail(MSOSM_ERR_ARG, "null input");
+    if (h->out_mode == MSOSM_OUT_NONE && !h->fold)
+        return h->fail(MSOSM_ERR_STATE, "no output mode and no fold attached");
+    cudaStream_t st = (cudaStream_t)stream;
+    // device input is read in place only when aligned to its element size (the
+    // kernels use 8/4/2-byte vector loads); anything else goes through staging
+    const bool dev = is_device_pointer(in) && ((uintptr_t)in % in_elem_bytes(h->in_format)) == 0;
+    const size_t step_bytes = (size_t)h->B * h->M * in_elem_bytes(h->in_format);
+    for (int s = 0; s < nsteps; s++)
+    {
+        int rc = process_one(h, (const char *)in + (size_t)s * step_bytes, dev, st);
+        if (rc != MSOSM_OK)
+            return rc;
+    }
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_output(msosm_t *h, void *out, void *stream)
+{
+    if (!h || !out)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "get_output before init");
+    const size_t n = (size_t)h->D * h->B * h->M;
+    cudaError_t e;
+    if (h->d_out_c64)
+        e = cudaMemcpyAsync(out, h->d_out_c64, n * sizeof(float2), cudaMemcpyDefault, (cudaStream_t)stream);
+    else if (h->d_out_u16)
+        e = cudaMemcpyAsync(out, h->d_out_u16, n * sizeof(uint32_t), cudaMemcpyDefault, (cudaStream_t)stream);
+    else
+        return h->fail(MSOSM_ERR_STATE, "no series output configured");
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "cudaMemcpyAsync(output)");
+    return MSOSM_OK;
+}
+
+extern "C" void *msosm_device_output(msosm_t *h) { return h ? (void *)h->d_out_c64 : nullptr; }
+extern "C" void *msosm_device_output_u16(msosm_t *h) { return h ? (void *)h->d_out_u16 : nullptr; }
+extern "C" long long msosm_steps(const msosm_t *h) { return h ? h->step : -1; }
+
+extern "C" int msosm_sync(msosm_t *h, void *stream)
+{
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return h ? h->cuda_fail(e, "cudaStreamSynchronize") : MSOSM_ERR_CUDA;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_destroy(msosm_t *h)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    delete h;
+    return MSOSM_OK;
+}
+
+extern "C" const char *msosm_last_error(const msosm_t *h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" int msosm_profile_enable(msosm_t *h, int on)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    h->prof.on = on != 0;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_profile_reset(msosm_t *h)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    h->prof.reset();
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
+                                  long long *transforms)
+{
+    if (!h || kind < 0 || kind >= Profiler::KINDS)
+        return MSOSM_ERR_ARG;
+    cudaError_t e = h->prof.collect();
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "cudaEventElapsedTime (kernel timing; sync the stream first)");
+    if (ms_total)
+        *ms_total = h->prof.ms[kind];
+    if (launches)
+        *launches = h->prof.launches[kind];
+    if (timed)
+        *timed = h->prof.timed[kind];
+    if (transforms)
+        *transforms = h->prof.transforms[kind];
+    return MSOSM_OK;
+}
+
+// ---- folding ------------------------------------------------------------------
+extern "C" int msosm_fold_create(float period, float fs, unsigned long size, unsigned long time_bin, int num_series,
+                                 msosm_fold_t **out)
+{
+    if (!out)
+        return MSOSM_ERR_ARG;
+    *out = nullptr;
+    if (!(period > 0) || !(fs > 0) || num_series <= 0)
+        return MSOSM_ERR_ARG;
+    msosm_fold_t *f = new (std::nothrow) msosm_fold_s();
+    if (!f)
+        return MSOSM_ERR_NOMEM;
+    f->period = period;
+    f->fs = fs;
+    f->P = (double)period;      // period_seconds (fold_gpu.cpp:9)
+    f->dt = 1.0 / (double)fs;   // fold_data_phase (fold_gpu.cpp:50)
+    f->size = size;
+    // period_samples = (unsigned long)(float)(period*fs) (fold_gpu.cpp:10-15)
+    const float psf = period * fs;
+    f->K = time_bin ? time_bin : (unsigned long)psf;
+    f->S = num_series;
+    if (f->K == 0 || f->K > (1ul << 30))
+    {
+        delete f;
+        return MSOSM_ERR_ARG;
+    }
+    const size_t n = (size_t)f->K * num_series;
+    if (dalloc(&f->d_sum, n) != cudaSuccess || dalloc(&f->d_cnt, n) != cudaSuccess ||
+        dalloc(&f->d_folded, n) != cudaSuccess)
+    {
+        cudaGetLastError();
+        delete f;
+        return MSOSM_ERR_NOMEM;
+    }
+    if (cudaMemset(f->d_sum, 0, n * sizeof(double)) != cudaSuccess ||
+        cudaMemset(f->d_cnt, 0, n * sizeof(unsigned long long)) != cudaSuccess)
+    {
+        delete f;
+        return MSOSM_ERR_CUDA;
+    }
+    *out = f;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_fold_accumulate(msosm_fold_t *f, const void *pol1, const void *pol2, void *stream)
+{
+    if (!f || !pol1)
+        return MSOSM_ERR_ARG;
+    cudaError_t e = msosm::launch_fold((const float2 *)pol1, (const float2 *)pol2, f->size, f->S, f->args(),
+                                       (cudaStream_t)stream);
+    if (e != cudaSuccess)
+    {
+        f->err = std::string("fold launch: ") + cudaGetErrorString(e);
+        return MSOSM_ERR_CUDA;
+    }
+    f->t_start += (double)f->size * f->dt; // fold_gpu.cpp:53
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_fold_read(msosm_fold_t *f, float *folded, double *sums, unsigned long long *counts,
+                               void *stream)
+{
+    if (!f)
+        return MSOSM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)f->K * f->S;
+    cudaError_t e = cudaSuccess;
+    if (folded)
+    {
+        e = msosm::launch_fold_finalize(f->d_sum, f->d_cnt, f->d_folded, n, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(folded, f->d_folded, n * sizeof(float), cudaMemcpyDefault, st);
+    }
+    if (e == cudaSuccess && sums)
+        e = cudaMemcpyAsync(sums, f->d_sum, n * sizeof(double), cudaMemcpyDefault, st);
+    if (e == cudaSuccess && counts)
+        e = cudaMemcpyAsync(counts, f->d_cnt, n * sizeof(unsigned long long), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+    {
+        f->err = std::string("fold read: ") + cudaGetErrorString(e);
+        return MSOSM_ERR_CUDA;
+    }
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_fold_reset(msosm_fold_t *f, void *stream)
+{
+    if (!f)
+        return MSOSM_ERR_ARG;
+    const size_t n = (size_t)f->K * f->S;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(f->d_sum, 0, n * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(f->d_cnt, 0, n * sizeof(unsigned long long), st) != cudaSuccess)
+        return MSOSM_ERR_CUDA;
+    f->t_start = 0.0;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_fold_dims(const msosm_fold_t *f, unsigned long *time_bin, int *num_series, unsigned long *size)
+{
+    if (!f)
+        return MSOSM_ERR_ARG;
+    if (time_bin)
+        *time_bin = f->K;
+    if (num_series)
+        *num_series = f->S;
+    if (size)
+        *size = f->size;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_fold_destroy(msosm_fold_t *f)
+{
+    if (!f)
+        return MSOSM_ERR_ARG;
+    delete f;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_attach_fold(msosm_t *h, msosm_fold_t *f)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (!f)
+    {
+        h->fold = nullptr;
+        return MSOSM_OK;
+    }
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "attach_fold before init");
+    if (f->S != h->D || f->size != (unsigned long)h->B * h->M)
+        return h->fail(MSOSM_ERR_ARG, "fold must have num_series == num_dms and size == B*M");
+    if (f->K > kMaxFusedBins)
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "fused fold supports at most 8192 bins");
+    h->fold = f;
+    return MSOSM_OK;
+}

@@ -1,0 +1,135 @@
+// Stand-alone intensity + phase fold (Fold_GPU, folding/fold_gpu.cpp:27-60).
+//
+// Replaces calculateIntensity / calculateIntensity_single (gpu/gpu_kernel.cu:477-507),
+// foldDataPhase (gpu_kernel.cu:509-543) and computeFoldedData (gpu_kernel.cu:545-565)
+// for callers that fold the processor's complex output themselves (the 2-pol
+// path and the reference-shaped Fold_GPU object).  The intensity is computed on
+// the fly -- no intensity buffer -- and samples are binned with the same Q0.64
+// fixed-point phase as the fused path: bin = floor(frac(t/P) * K) computed
+// without per-sample FP64 arithmetic.
+#include "msosm_common.cuh"
+
+namespace msosm {
+
+constexpr int FOLD_THREADS = 256;
+constexpr unsigned FOLD_SMEM_MAX_BINS = 12288; // 96 KB of bins
+
+template <bool TWO_POL, bool SMEM_BINS>
+__global__ void __launch_bounds__(FOLD_THREADS)
+    fold_kernel(const float2 *__restrict__ a, const float2 *__restrict__ b, size_t size, FoldArgs f, size_t chunk)
+{
+    extern __shared__ float fsm[];
+    float *s_sum = fsm;
+    unsigned *s_cnt = reinterpret_cast<unsigned *>(fsm + (SMEM_BINS ? f.K : 0));
+    const int s = blockIdx.y;
+    const float2 *pa = a + (size_t)s * size;
+    const float2 *pb = TWO_POL ? b + (size_t)s * size : nullptr;
+    if constexpr (SMEM_BINS)
+    {
+        for (unsigned i = threadIdx.x; i < f.K; i += FOLD_THREADS)
+        {
+            s_sum[i] = 0.0f;
+            s_cnt[i] = 0u;
+        }
+        __syncthreads();
+    }
+    const size_t begin = (size_t)blockIdx.x * chunk;
+    const size_t end = begin + chunk < size ? begin + chunk : size;
+    // whole warps iterate together so the shuffles in fold_accumulate see all lanes
+    for (size_t base = begin; base < end; base += FOLD_THREADS)
+    {
+        const size_t i = base + threadIdx.x;
+        float p = 0.0f;
+        unsigned bin = 0;
+        if (i < end)
+        {
+            const float2 x = __ldcs(pa + i);
+            if constexpr (TWO_POL)
+            {
+                const float2 y = __ldcs(pb + i);
+                p = sqrtf(x.x * x.x + x.y * x.y + y.x * y.x + y.y * y.y);
+            }
+            else
+                p = x.x * x.x + x.y * x.y;
+            bin = phase_bin(f.phase0 + (uint64_t)i * f.dphase, f.K);
+        }
+        if constexpr (SMEM_BINS)
+            fold_accumulate(s_sum, s_cnt, bin, p);
+        else if (p != 0.0f)
+        {
+            atomicAdd(f.sum + (size_t)s * f.K + bin, (double)p);
+            atomicAdd(f.cnt + (size_t)s * f.K + bin, 1ULL);
+        }
+    }
+    if constexpr (SMEM_BINS)
+    {
+        __syncthreads();
+        double *gs = f.sum + (size_t)s * f.K;
+        unsigned long long *gc = f.cnt + (size_t)s * f.K;
+        for (unsigned k = threadIdx.x; k < f.K; k += FOLD_THREADS)
+        {
+            const unsigned c = s_cnt[k];
+            if (c)
+            {
+                atomicAdd(gs + k, (double)s_sum[k]);
+                atomicAdd(gc + k, (unsigned long long)c);
+            }
+        }
+    }
+}
+
+template <bool TWO_POL, bool SMEM_BINS>
+static cudaError_t fold_launch(const float2 *a, const float2 *b, size_t size, int series, const FoldArgs &f,
+                               cudaStream_t st)
+{
+    auto k = fold_kernel<TWO_POL, SMEM_BINS>;
+    const size_t smem = SMEM_BINS ? (size_t)f.K * 8 : 0;
+    cudaError_t e = ensure_smem(k, smem);
+    if (e != cudaSuccess)
+        return e;
+    // ~4 chunks per SM across all series; each chunk a multiple of the block size
+    const size_t target_blocks = 152 * 4;
+    size_t per_series = (target_blocks + series - 1) / series;
+    size_t chunk = (size + per_series - 1) / per_series;
+    chunk = ((chunk + FOLD_THREADS - 1) / FOLD_THREADS) * FOLD_THREADS;
+    if (chunk < 8 * FOLD_THREADS)
+        chunk = 8 * FOLD_THREADS;
+    const unsigned gx = (unsigned)((size + chunk - 1) / chunk);
+    dim3 grid(gx > 0 ? gx : 1, series);
+    k<<<grid, FOLD_THREADS, smem, st>>>(a, b, size, f, chunk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fold(const float2 *pol1, const float2 *pol2, size_t size, int series, const FoldArgs &f,
+                        cudaStream_t st)
+{
+    if (size == 0 || series <= 0)
+        return cudaSuccess;
+    const bool smem_bins = f.K <= FOLD_SMEM_MAX_BINS;
+    if (pol2)
+        return smem_bins ? fold_launch<true, true>(pol1, pol2, size, series, f, st)
+                         : fold_launch<true, false>(pol1, pol2, size, series, f, st);
+    return smem_bins ? fold_launch<false, true>(pol1, nullptr, size, series, f, st)
+                     : fold_launch<false, false>(pol1, nullptr, size, series, f, st);
+}
+
+__global__ void fold_finalize_kernel(const double *__restrict__ sum, const unsigned long long *__restrict__ cnt,
+                                     float *__restrict__ folded, size_t n)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const unsigned long long c = cnt[i];
+    folded[i] = c > 0 ? (float)(sum[i] / (double)c) : 0.0f;
+}
+
+cudaError_t launch_fold_finalize(const double *sum, const unsigned long long *cnt, float *folded, size_t n,
+                                 cudaStream_t st)
+{
+    if (n == 0)
+        return cudaSuccess;
+    fold_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(sum, cnt, folded, n);
+    return cudaGetLastError();
+}
+
+} // namespace msosm

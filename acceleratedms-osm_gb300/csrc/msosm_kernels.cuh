@@ -1,0 +1,83 @@
+// Kernel launch interface of the MS-OSM engine (internal; not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace msosm {
+
+enum InFormat : int
+{
+    IN_U16 = 0, // uint16_pair offset binary, 0 = no data (gpu_kernel.cu:16-30)
+    IN_C64 = 1, // complex64
+    IN_I8 = 2,  // int8 interleaved I/Q
+};
+
+enum OutMode : int
+{
+    OUT_NONE = 0,
+    OUT_C64 = 1,  // float2 [D][B][M] (fold-mode output buffer of the reference)
+    OUT_U16 = 2,  // uint16_pair [D][B][M] (discardSamplesToUint16)
+    OUT_FOLD = 4, // |x|^2 phase fold of every DM (fused)
+};
+
+// F = N1 * N2, N2 = 2^ceil(L/2), N1 = 2^floor(L/2).
+struct Geom
+{
+    int L, F, M, N1, N2;
+};
+
+// Twiddle tables for one transform direction, in device memory.
+struct Twiddles
+{
+    const float2 *twN1; // W_{N1}^m, m < N1
+    const float2 *twN2; // W_{N2}^m, m < N2
+    const float2 *lo;   // W_F^m, m < N2
+    const float2 *hi;   // W_F^(m*N2), m < N1
+};
+
+struct FoldArgs
+{
+    double *sum;         // [D][K] accumulated sums (double, as Fold_GPU)
+    unsigned long long *cnt; // [D][K] sample counts
+    uint64_t phase0;     // phase of sample 0 of this call, Q0.64 turns
+    uint64_t dphase;     // phase advance per sample, Q0.64 turns
+    unsigned K;          // bins per series
+};
+
+// Forward: B overlapping windows of the [tail | new input] stream -> spectra ring slots.
+// Pass 1 (decode + column transforms -> T), pass 2 (row transforms -> ring slot rbi+b).
+cudaError_t launch_forward_p1(const Geom &g, const Twiddles &tw, int in_format, const void *in, const float2 *tail,
+                              float2 *tail_next, float2 *T, int B, cudaStream_t st);
+cudaError_t launch_forward_p2(const Geom &g, const Twiddles &tw, const float2 *T, float2 *ring, int rbi, int B,
+                              cudaStream_t st);
+
+// Inverse for FFTs g0 .. g0+count-1 (g = d*B + b): gather x response -> inverse -> epilogue.
+struct InvArgs
+{
+    const float2 *ring;
+    const float2 *H;        // [D][F]
+    const uint16_t *delays; // [D][F]
+    float2 *T;              // [count][F] intermediate
+    int rbi, fbs, B;
+    int out_mode;
+    float2 *out_c64;  // [D][B][M]
+    uint32_t *out_u16; // [D][B][M]
+    FoldArgs fold;
+};
+// Pass 1 (gather x response + column transforms -> T), pass 2 (row transforms + epilogue).
+cudaError_t launch_inverse_p1(const Geom &g, const Twiddles &tw, const InvArgs &a, long long g0, int count,
+                              cudaStream_t st);
+cudaError_t launch_inverse_p2(const Geom &g, const Twiddles &tw, const InvArgs &a, long long g0, int count,
+                              cudaStream_t st);
+
+// Standalone intensity + phase fold of `size` samples of one or two complex series
+// (Fold_GPU::calculate_intensity + fold_data_phase).  pol2 == nullptr: |a|^2, else
+// sqrt(|a|^2+|b|^2).  series: number of consecutive series of length `size`.
+cudaError_t launch_fold(const float2 *pol1, const float2 *pol2, size_t size, int series, const FoldArgs &f,
+                        cudaStream_t st);
+
+// folded[i] = cnt ? sum/cnt : 0 (computeFoldedData_kernel)
+cudaError_t launch_fold_finalize(const double *sum, const unsigned long long *cnt, float *folded, size_t n,
+                                 cudaStream_t st);
+
+} // namespace msosm

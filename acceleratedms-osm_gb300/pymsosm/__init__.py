@@ -1,0 +1,340 @@
+"""Python binding of the GB300 MS-OSM engine's C ABI (include/msosm_gb300.h).
+
+A thin ctypes layer used by the test-suite and bench.py: it loads the in-tree
+shared library (acceleratedms-osm_gb300/lib/libmsosm_gb300.so) and raises if
+it is missing -- there is no CPU fallback.  Device buffers may be passed as
+integers (raw device pointers) or as torch CUDA tensors; host buffers as numpy
+arrays or pinned torch CPU tensors.
+
+Class names follow the reference's processors:
+  MsosmGpuBatch  ~ MSOSM_GPU_BATCH (dedispersion/include/msosm_gpu_batch.h:13-97)
+  OsmGpuBatch    ~ OSM_GPU_BATCH   (dedispersion/include/osm_gpu_batch.h:7-38)
+  FoldGpu        ~ Fold_GPU        (folding/include/fold_gpu.h:10-43)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parents[1]
+LIB_PATH = PKG / "lib" / "libmsosm_gb300.so"
+HEADER = PKG.parent / "include" / "msosm_gb300.h"
+
+OK = 0
+IN_U16, IN_C64, IN_I8 = 0, 1, 2
+OUT_NONE, OUT_C64, OUT_U16 = 0, 1, 2
+IN_BYTES = {IN_U16: 4, IN_C64: 8, IN_I8: 2}
+
+_lib = None
+
+
+class MsosmError(RuntimeError):
+    pass
+
+
+def build(force: bool = False) -> Path:
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_msosm_build", PKG / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def declared_functions() -> list[str]:
+    """Function names declared in include/msosm_gb300.h."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:msosm|osm)_[a-z0-9_]+)\s*\(", text)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise MsosmError(f"{LIB_PATH} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+        L = C.CDLL(str(LIB_PATH))
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+P, I, F, D, UL, LL = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_ulong, C.c_longlong
+PI = C.POINTER(C.c_int)
+
+
+def _declare(L):
+    L.msosm_version.restype = C.c_char_p
+    L.msosm_status_string.restype = C.c_char_p
+    L.msosm_status_string.argtypes = [I]
+    L.msosm_create.argtypes = [F, F, P, I, C.POINTER(P)]
+    L.osm_create.argtypes = [F, F, F, C.POINTER(P)]
+    L.msosm_init.argtypes = [P, I, I, I, I]
+    L.msosm_get_dims.argtypes = [P, PI, PI, PI, PI, PI, PI, PI]
+    L.msosm_get_nd.argtypes = [P, P]
+    L.msosm_get_delaycounts.argtypes = [P, P]
+    L.msosm_get_delay_points.argtypes = [P, I, P]
+    L.msosm_get_response.argtypes = [P, I, P]
+    L.msosm_process.argtypes = [P, P, P]
+    L.msosm_process_many.argtypes = [P, P, I, P]
+    L.msosm_get_output.argtypes = [P, P, P]
+    L.msosm_device_output.restype = P
+    L.msosm_device_output.argtypes = [P]
+    L.msosm_device_output_u16.restype = P
+    L.msosm_device_output_u16.argtypes = [P]
+    L.msosm_steps.restype = LL
+    L.msosm_steps.argtypes = [P]
+    L.msosm_sync.argtypes = [P, P]
+    L.msosm_destroy.argtypes = [P]
+    L.msosm_last_error.restype = C.c_char_p
+    L.msosm_last_error.argtypes = [P]
+    L.msosm_fold_create.argtypes = [F, F, UL, UL, I, C.POINTER(P)]
+    L.msosm_fold_accumulate.argtypes = [P, P, P, P]
+    L.msosm_fold_read.argtypes = [P, P, P, P, P]
+    L.msosm_fold_reset.argtypes = [P, P]
+    L.msosm_fold_dims.argtypes = [P, C.POINTER(UL), PI, C.POINTER(UL)]
+    L.msosm_fold_destroy.argtypes = [P]
+    L.msosm_attach_fold.argtypes = [P, P]
+    L.msosm_profile_enable.argtypes = [P, I]
+    L.msosm_profile_reset.argtypes = [P]
+    L.msosm_profile_read.argtypes = [P, I, C.POINTER(D), C.POINTER(LL), C.POINTER(LL), C.POINTER(LL)]
+    L.msosm_plan_nd.argtypes = [F, F, P, I, P]
+    L.msosm_plan_min_order.argtypes = [P, I, P]
+    L.msosm_plan_segmentation.argtypes = [F, F, F, I, I, P, P]
+    L.msosm_plan_response.argtypes = [F, F, F, I, P]
+    L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
+
+
+def plan_nd(bw, f0, dms) -> np.ndarray:
+    d = np.ascontiguousarray(np.atleast_1d(np.asarray(dms, np.float32)))
+    out = np.zeros(len(d), np.int32)
+    if lib().msosm_plan_nd(bw, f0, d.ctypes.data, len(d), out.ctypes.data) != OK:
+        raise MsosmError("msosm_plan_nd")
+    return out
+
+
+def plan_min_order(nd) -> int:
+    a = np.ascontiguousarray(np.atleast_1d(np.asarray(nd, np.int32)))
+    m = np.zeros(1, np.int32)
+    if lib().msosm_plan_min_order(a.ctypes.data, len(a), m.ctypes.data) != OK:
+        raise MsosmError("msosm_plan_min_order")
+    return int(m[0])
+
+
+def plan_segmentation(bw, f0, dm, nd, M):
+    d = np.zeros(2 * M, np.int32)
+    dc = np.zeros(1, np.int32)
+    if lib().msosm_plan_segmentation(bw, f0, dm, nd, M, d.ctypes.data, dc.ctypes.data) != OK:
+        raise MsosmError("msosm_plan_segmentation")
+    return d, int(dc[0])
+
+
+def plan_response(bw, f0, dm, M) -> np.ndarray:
+    H = np.zeros(2 * M, np.complex64)
+    if lib().msosm_plan_response(bw, f0, dm, M, H.ctypes.data) != OK:
+        raise MsosmError("msosm_plan_response")
+    return H
+
+
+def osm_plan(bw, dm, f0):
+    nd, mm = C.c_ulong(), C.c_ulong()
+    lib().osm_plan(bw, dm, f0, C.byref(nd), C.byref(mm))
+    return nd.value, mm.value
+
+
+def _ptr(x):
+    """Raw address of a numpy array, torch tensor, int or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class MsosmGpuBatch:
+    """MS-OSM processor over many DM trials (MSOSM_GPU_BATCH)."""
+
+    def __init__(self, bw: float, dms, f0: float, *, _osm_dm: float | None = None):
+        L = lib()
+        self._h = P()
+        if _osm_dm is None:
+            d = np.ascontiguousarray(np.atleast_1d(np.asarray(dms, dtype=np.float32)))
+            rc = L.msosm_create(bw, f0, d.ctypes.data, len(d), C.byref(self._h))
+            self.dms = d
+        else:
+            rc = L.osm_create(bw, _osm_dm, f0, C.byref(self._h))
+            self.dms = np.array([_osm_dm], np.float32)
+        if rc != OK:
+            raise MsosmError(f"create failed: {L.msosm_status_string(rc).decode()}")
+        self.num_dms = len(self.dms)
+        self.nd = np.zeros(self.num_dms, np.int32)
+        L.msosm_get_nd(self._h, self.nd.ctypes.data)
+        self._fold = None
+        self.inited = False
+
+    # -- reference-shaped API ------------------------------------------------
+    def initialize(self, fftpoint: int = 0, batch: int = 1, in_format: int = IN_U16, out_mode: int = OUT_C64):
+        self._check(lib().msosm_init(self._h, fftpoint, batch, in_format, out_mode))
+        self.in_format, self.out_mode = in_format, out_mode
+        vals = [C.c_int() for _ in range(7)]
+        lib().msosm_get_dims(self._h, *[C.byref(v) for v in vals])
+        (self.M, self.M_min, self.fftpoint, self.batch, self.num_dms, self.delaycount,
+         self.ring_blocks) = [v.value for v in vals]
+        self.inited = True
+        return self
+
+    def filter_block(self, data, stream=None):
+        """One step: batch*M samples (host array/pinned tensor or device tensor)."""
+        self._check(lib().msosm_process(self._h, _ptr(data), _stream(stream)))
+
+    def filter_blocks(self, data, nsteps: int, stream=None):
+        self._check(lib().msosm_process_many(self._h, _ptr(data), nsteps, _stream(stream)))
+
+    def get_output(self, out, stream=None):
+        self._check(lib().msosm_get_output(self._h, _ptr(out), _stream(stream)))
+
+    def get_output_pointer(self) -> int:
+        return lib().msosm_device_output(self._h) or 0
+
+    def get_output_pointer_u16(self) -> int:
+        return lib().msosm_device_output_u16(self._h) or 0
+
+    def synchronize(self, stream=None):
+        self._check(lib().msosm_sync(self._h, _stream(stream)))
+
+    def attach_fold(self, fold: "FoldGpu | None"):
+        self._check(lib().msosm_attach_fold(self._h, fold._h if fold is not None else None))
+        self._fold = fold
+
+    # -- kernel timing ------------------------------------------------------
+    KERNELS = ("fwd_pass1", "fwd_pass2", "inv_pass1", "inv_pass2")
+
+    def profile(self, on: bool = True):
+        self._check(lib().msosm_profile_enable(self._h, 1 if on else 0))
+
+    def profile_reset(self):
+        self._check(lib().msosm_profile_reset(self._h))
+
+    def profile_read(self) -> dict:
+        """{kernel: dict(ms, launches, timed, transforms)}; sync the stream first."""
+        out = {}
+        for k, name in enumerate(self.KERNELS):
+            ms, n, t, tr = D(), LL(), LL(), LL()
+            self._check(lib().msosm_profile_read(self._h, k, C.byref(ms), C.byref(n), C.byref(t), C.byref(tr)))
+            out[name] = dict(ms=ms.value, launches=n.value, timed=t.value, transforms=tr.value)
+        return out
+
+    # -- planning results --------------------------------------------------
+    @property
+    def steps(self) -> int:
+        return lib().msosm_steps(self._h)
+
+    def delaycounts(self) -> np.ndarray:
+        out = np.zeros(self.num_dms, np.int32)
+        self._check(lib().msosm_get_delaycounts(self._h, out.ctypes.data))
+        return out
+
+    def delay_points(self, i: int) -> np.ndarray:
+        out = np.zeros(self.fftpoint, np.int32)
+        self._check(lib().msosm_get_delay_points(self._h, i, out.ctypes.data))
+        return out
+
+    def response(self, i: int) -> np.ndarray:
+        out = np.zeros(self.fftpoint, np.complex64)
+        self._check(lib().msosm_get_response(self._h, i, out.ctypes.data))
+        return out
+
+    def samples_per_step(self) -> int:
+        return self.batch * self.M
+
+    def _check(self, rc):
+        if rc != OK:
+            msg = lib().msosm_last_error(self._h)
+            raise MsosmError(f"{lib().msosm_status_string(rc).decode()}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self._h:
+            lib().msosm_destroy(self._h)
+            self._h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OsmGpuBatch(MsosmGpuBatch):
+    """Plain overlap-save, single DM (OSM_GPU_BATCH)."""
+
+    def __init__(self, bw: float, dm: float, f0: float):
+        super().__init__(bw, None, f0, _osm_dm=dm)
+
+
+class FoldGpu:
+    """Intensity + phase fold (Fold_GPU), for num_series independent series."""
+
+    def __init__(self, period: float, fs: float, size: int, time_bin: int = 0, num_series: int = 1):
+        L = lib()
+        self._h = P()
+        rc = L.msosm_fold_create(period, fs, size, time_bin, num_series, C.byref(self._h))
+        if rc != OK:
+            raise MsosmError(f"fold create failed: {L.msosm_status_string(rc).decode()}")
+        K = C.c_ulong()
+        S = C.c_int()
+        Z = C.c_ulong()
+        L.msosm_fold_dims(self._h, C.byref(K), C.byref(S), C.byref(Z))
+        self.time_bin, self.num_series, self.size = K.value, S.value, Z.value
+
+    def accumulate(self, pol1, pol2=None, stream=None):
+        rc = lib().msosm_fold_accumulate(self._h, _ptr(pol1), _ptr(pol2), _stream(stream))
+        if rc != OK:
+            raise MsosmError(f"fold accumulate: {lib().msosm_status_string(rc).decode()}")
+
+    def read(self, stream=None):
+        shape = (self.num_series, self.time_bin)
+        folded = np.zeros(shape, np.float32)
+        sums = np.zeros(shape, np.float64)
+        cnts = np.zeros(shape, np.uint64)
+        rc = lib().msosm_fold_read(self._h, folded.ctypes.data, sums.ctypes.data, cnts.ctypes.data,
+                                   _stream(stream))
+        if rc != OK:
+            raise MsosmError(f"fold read: {lib().msosm_status_string(rc).decode()}")
+        return folded, sums, cnts
+
+    def read_folded(self, out: np.ndarray, stream=None):
+        """Folded means only, into a caller-owned float32 [num_series][time_bin] array."""
+        assert out.dtype == np.float32 and out.size == self.num_series * self.time_bin
+        rc = lib().msosm_fold_read(self._h, out.ctypes.data, None, None, _stream(stream))
+        if rc != OK:
+            raise MsosmError(f"fold read: {lib().msosm_status_string(rc).decode()}")
+        return out
+
+    def reset(self, stream=None):
+        lib().msosm_fold_reset(self._h, _stream(stream))
+
+    def close(self):
+        if self._h:
+            lib().msosm_fold_destroy(self._h)
+            self._h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the MS-OSM hot path on GB300.
+
+Workload (the many-DM configuration): complex64 single-pol baseband, 64 MHz
+bandwidth at 1400 MHz centre (f0 = 1368 MHz), 2^26 samples with a pulsar
+(period 33 ms, 5 % duty, -10 dB per-sample SNR) injected at DM 123.4; 512 DM
+trials uniformly spaced in 0..200 pc/cm^3; FFT size 2^18 (M = 2^17), batch 32
+windows per call; every trial folded into 512 phase bins (no series output).
+
+One "step" = one pass of the engine over the whole 2^26-sample baseband
+(16 calls of 2^22 samples), all 512 trials dedispersed and folded.
+
+  value   samples x DM trials per second with the input resident in HBM
+          (CUDA events on the launch stream, max over ranks).
+  e2e     the same through the C ABI with the input in pinned HOST memory:
+          every step copies its 512 MB in and reads the folded profiles back.
+  roofline  the dominant kernel's achieved bandwidth under the algorithmic
+          byte model of 16 B per sample x DM, from per-launch CUDA events taken
+          inside the timed region, against the measured HBM copy bandwidth.
+  cpu_baseline  the FP32 CPU port of the same algorithm (oracle/) on a bounded
+          sample, all host threads.
+
+`--impl reference` times that CPU implementation alone (the reference has no
+CPU MS-OSM path of its own; its planning code is x86-build-only here).
+Multi-GPU (torchrun): each rank dedisperses its own interleaved share of a
+512*N-trial grid (weak scaling, no data-path collective); the host-side barrier
+and the max-over-ranks reduction use gloo.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "acceleratedms-osm_gb300"))
+
+METRIC = "baseband samples/s x DM trials"
+UNIT = "sample*DM/s"
+BYTES_PER_UNIT = 16  # algorithmic bytes per sample x DM (fold-only), see the design doc
+
+WORKLOADS = {
+    "many_dm_512": dict(bw=64e6, centre=1400e6, n_dms=512, dm_lo=0.0, dm_hi=200.0, fftpoint=1 << 18, batch=32,
+                        nbins=512, samples=1 << 26, period=0.033, inject_dm=123.4, snr_db=-10.0, duty=0.05),
+    "single_dm_50": dict(bw=16e6, centre=1400e6, n_dms=1, dm_lo=50.0, dm_hi=50.0, fftpoint=1 << 16, batch=32,
+                         nbins=256, samples=1 << 22, period=0.033, inject_dm=50.0, snr_db=-10.0, duty=0.05),
+}
+
+
+def dm_grid(w, rank=0, world=1):
+    if w["n_dms"] == 1:
+        return np.array([w["dm_lo"]], np.float32)
+    g = np.linspace(w["dm_lo"], w["dm_hi"], w["n_dms"] * world).astype(np.float32)
+    return np.ascontiguousarray(g[rank::world])
+
+
+def f0_of(w):
+    return np.float32(np.float32(w["centre"]) - np.float32(w["bw"]) / np.float32(2))
+
+
+# ----------------------------------------------------------------------------
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per F-point transform of `kernel` from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.f = None
+
+    def _gpu_id(self):
+        try:
+            import torch
+
+            p = torch.cuda.get_device_properties(self.dev)
+            return f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0"
+        except Exception:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            return vis.split(",")[self.dev] if vis else str(self.dev)
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self._gpu_id()], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------
+def cpu_port_rate(w, n_dms_sample: int, substeps: int, seed: int = 3, steps: int = 1, warmup: int = 0):
+    """FP32 CPU port (oracle/) on a bounded sample: returns (rate, seconds, description)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    oracle.build()
+    bw, f0 = np.float32(w["bw"]), f0_of(w)
+    grid = dm_grid(w)
+    pick = np.linspace(0, len(grid) - 1, min(n_dms_sample, len(grid))).round().astype(int)
+    dms = grid[np.unique(pick)]
+    plan = oracle.Plan(bw, f0, dms, w["fftpoint"], batch=w["batch"])
+    m = oracle.Msosm(plan, w["batch"], fp64=False, H=plan.H.astype(np.complex64))
+    m.set_fold(w["nbins"], np.float32(w["period"]), bw)
+    n = w["batch"] * plan.M
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex64)
+    for _ in range(warmup):
+        m.process(x, want_output=False)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        for _ in range(substeps):
+            m.process(x, want_output=False)
+        times.append(time.perf_counter() - t0)
+    units = substeps * n * len(dms)
+    sec = float(np.mean(times))
+    desc = (f"{len(dms)} of the {len(grid)} DM trials x {substeps} calls of {n} samples "
+            f"({units:.3g} sample*DM), FP32, fold-only, {m.nthreads} threads")
+    return units / sec, sec, desc, m.nthreads, times
+
+
+def run_reference(args, w, rank, world):
+    if rank != 0:
+        return
+    n_dms_sample = 32
+    substeps = 2
+    rate, sec, desc, cores, times = cpu_port_rate(w, n_dms_sample, substeps, steps=args.steps, warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, **{k: v for k, v in w.items()}},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference implements MS-OSM only on the GPU (cuFFT); its CPU implementation of the path "
+                 "is the project's FP32 restatement of the same algorithm (oracle/), timed here"),
+    }
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------
+def run_engine(args, w, rank, world, local):
+    import torch
+
+    import pymsosm as eng
+    from pymsosm.simulate import pulsar_signal
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    bw, f0 = np.float32(w["bw"]), f0_of(w)
+    dms = dm_grid(w, rank, world)
+    N = w["samples"]
+
+    x = pulsar_signal(N, float(bw), float(f0), w["inject_dm"], w["period"], duty=w["duty"],
+                      snr_db=w["snr_db"], seed=2 + rank)
+    host = torch.from_numpy(x.view(np.float32)).pin_memory()
+    dinp = host.to(dev)
+    del x
+
+    proc = eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_C64, eng.OUT_NONE)
+    step_n = proc.batch * proc.M
+    calls = N // step_n
+    fold = eng.FoldGpu(np.float32(w["period"]), bw, step_n, w["nbins"], len(dms))
+    proc.attach_fold(fold)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(src):
+        proc.filter_blocks(src, calls, stream)
+
+    # warm-up (also compiles nothing: kernels are prebuilt)
+    for _ in range(args.warmup):
+        step(dinp)
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident input ------------------------------
+    proc.profile_reset()
+    proc.profile(True)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(dinp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    proc.profile(False)
+    t_ms = ev0.elapsed_time(ev1)
+    t_ms = reduce_max(t_ms, world)
+    units_per_step_rank = N * len(dms)
+    total_units = reduce_sum(units_per_step_rank * args.steps, world)
+    value = total_units / (t_ms * 1e-3)
+    prof = proc.profile_read()
+    launches = sum(v["launches"] for v in prof.values())
+
+    # roofline of the dominant kernel (largest summed device time)
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    pk = prof[dom]
+    per_launch_ms = pk["ms"] / max(pk["timed"], 1)
+    trans_per_launch = pk["transforms"] / max(pk["launches"], 1)
+    bytes_per_launch = BYTES_PER_UNIT * proc.M * trans_per_launch
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_src = measured_peak()
+    tr = profile_traffic(dom)
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": f"of {peak_src}",
+        "traffic": (tr * trans_per_launch) if tr is not None else None,
+        "bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms,
+        "pipeline_achieved": BYTES_PER_UNIT * units_per_step_rank * args.steps / (t_ms * 1e-3) / 1e9,
+        "kernel_share": {k: v["ms"] / max(sum(p["ms"] for p in prof.values()), 1e-9) for k, v in prof.items()},
+    }
+
+    # ---- end-to-end through the C ABI from pinned host memory -------------
+    folded_host = np.zeros((len(dms), w["nbins"]), np.float32)
+    proc.filter_blocks(host, calls, stream)  # one untimed e2e warm-up step
+    fold.read_folded(folded_host, stream)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        proc.filter_blocks(host, calls, stream)
+        fold.read_folded(folded_host, stream)  # D2H of the step's result (synchronises)
+    torch.cuda.synchronize()
+    e_ms = (time.perf_counter() - e0) * 1e3
+    barrier(world)
+    e_ms = reduce_max(e_ms, world)
+    e2e = {"value": total_units / (e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(host.numel() * 4),
+           "d2h_bytes_per_step": int(folded_host.nbytes)}
+
+    # ---- sanity: the injected DM is recovered ------------------------------
+    def snr(p):
+        base = np.median(p)
+        mad = np.median(np.abs(p - base)) * 1.4826
+        return float((p.max() - base) / mad) if mad > 0 else 0.0
+
+    s = np.array([snr(p) for p in folded_host])
+    best = int(np.argmax(s))
+    check = {"best_dm": float(dms[best]), "snr_best": float(s[best]), "snr_dm_lowest": float(s[0]),
+             "injected_dm": w["inject_dm"]}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "dm_trials_per_gpu": len(dms), "fft_size": proc.fftpoint,
+                   "M": proc.M, "batch": proc.batch, "samples": N, "phase_bins": w["nbins"],
+                   "bandwidth_hz": float(bw), "f0_hz": float(f0), "input": "complex64, 1 pol",
+                   "l2": "inputs larger than L2 (512 MB baseband, 1 GB responses, 128 MB spectra ring)",
+                   "parallelism": f"dm-shard x{world}"},
+        "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "check": check,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        rate, sec, desc, cores, _ = cpu_port_rate(w, 64, 4)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="many_dm_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    w = WORKLOADS[args.workload]
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+    else:
+        run_engine(args, w, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * msosm_gb300.h -- C ABI of the GB300-native MS-OSM coherent-dedispersion engine.
+ *
+ * This is the drop-in boundary for the hot path of joezhouchenye/AcceleratedMS-OSM:
+ * host code (the header-only C++ shim in include/compat/, or any FFI) calls these
+ * functions; they drive hand-written sm_103a kernels on one GPU.  Plain pointers
+ * and sizes only; no CUDA or torch types appear (streams are passed as void*,
+ * meaning cudaStream_t, NULL = the legacy default stream).
+ *
+ * Every function returns an int status (MSOSM_OK = 0).  Nothing here calls
+ * exit() or resets the device, unlike the reference's CUDA_CHECK / destructor
+ * (gpu/include/gpu_common.cuh:42-62, dedispersion/msosm/msosm_gpu_batch.cpp:252-260).
+ * msosm_last_error() returns the message of a handle's last failure.
+ *
+ * Threading: a handle is driven by one host thread at a time (the reference's
+ * processor objects have the same rule).  All device work of a handle is ordered
+ * on the stream passed to each call.
+ */
+#ifndef MSOSM_GB300_H
+#define MSOSM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define MSOSM_OK 0
+#define MSOSM_ERR_ARG 1         /* invalid argument */
+#define MSOSM_ERR_STATE 2       /* call out of order (e.g. process before init) */
+#define MSOSM_ERR_CUDA 3        /* a CUDA runtime call or kernel launch failed */
+#define MSOSM_ERR_NOMEM 4       /* device or host allocation failed */
+#define MSOSM_ERR_UNSUPPORTED 5 /* size/format outside what the engine supports */
+
+/* ---- input sample formats (one complex sample per element) ----------------- */
+#define MSOSM_IN_U16 0 /* uint16_pair, offset binary, 0 = no data (utils/include/globals.h:22-26) */
+#define MSOSM_IN_C64 1 /* complex64 (float re, float im) */
+#define MSOSM_IN_I8 2  /* int8 interleaved I/Q (psrdada NBIT=8) */
+
+/* ---- output modes (bit flags) ----------------------------------------------- */
+#define MSOSM_OUT_NONE 0 /* no series output (fold-only; needs an attached fold) */
+#define MSOSM_OUT_C64 1  /* complex64 [D][B][M] -- the reference's fold-mode output_buffer_d */
+#define MSOSM_OUT_U16 2  /* uint16_pair [D][B][M] -- the reference's stream-mode output */
+
+typedef struct msosm_s msosm_t;
+typedef struct msosm_fold_s msosm_fold_t;
+
+/* Library version string and the text of a status code. */
+const char *msosm_version(void);
+const char *msosm_status_string(int status);
+
+/* ---- host-only planning (no GPU needed) -------------------------------------
+ * The reference's Prepare_MSOSM / Prepare_OSM public methods as free functions:
+ * msosm_plan_nd        Nd per DM, Prepare_MSOSM ctor (msosm_prepare.cpp:25-46)
+ * msosm_plan_min_order calculate_min_order (msosm_prepare.cpp:48-69): M_min
+ * msosm_plan_segmentation segmentation(i) (msosm_prepare.cpp:215-284): 2M
+ *                      per-bin block delays and the DM's delaycount
+ * msosm_plan_response  generate_dedisp_params(i) (msosm_prepare.cpp:107-164):
+ *                      2M complex64 (4M floats), FP64 inside
+ * osm_plan             Prepare_OSM ctor + calculate_min_order (osm_prepare.cpp:3-28)
+ */
+int msosm_plan_nd(float bw, float f0, const float *dms, int num_dms, int *nd_out);
+int msosm_plan_min_order(const int *nd, int num_dms, int *M_min_out);
+int msosm_plan_segmentation(float bw, float f0, float dm, int nd, int M, int *delay_out, int *dc_out);
+int msosm_plan_response(float bw, float f0, float dm, int M, float *H_out);
+int osm_plan(float bw, float dm, float f0, unsigned long *nd_out, unsigned long *M_min_out);
+
+/* ---- MS-OSM processor --------------------------------------------------------
+ * msosm_create replaces Prepare_MSOSM(float bw, float *dm, float f0, int numDMs)
+ *   (dedispersion/include/msosm_prepare.h:13, msosm_prepare.cpp:25-46) and the
+ *   MSOSM_GPU_BATCH constructors (dedispersion/include/msosm_gpu_batch.h:16-17).
+ *   bw = sampling rate = bandwidth in Hz, f0 = band bottom in Hz, dms copied.
+ *   DMs must be ascending (the reference reads past its boundary table
+ *   otherwise, msosm_prepare.cpp:239); DM 0 is an identity filter.
+ * msosm_init replaces MSOSM_GPU_BATCH::initialize_uint16(int fftpoint, int batch,
+ *   bool fold) (msosm_gpu_batch.h:19, msosm_gpu_batch.cpp:12-151): fftpoint 0
+ *   picks 2*M_min, otherwise M = max(fftpoint/2, M_min).  in_format is an
+ *   MSOSM_IN_* value, out_mode an MSOSM_OUT_* mask.  batch need not be a
+ *   multiple of 4.  fftpoint must come out a power of two in [256, 2^22].
+ */
+int msosm_create(float bw, float f0, const float *dms, int num_dms, msosm_t **out);
+int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, int out_mode);
+
+/* Planning results: M, M_min, F = 2M, batch, DM count, processor-wide delaycount
+ * and the number of spectra kept in the ring (fft_block_size).  Any pointer may
+ * be NULL.  Replaces the public members M, M_min, numDMs, delaycount of
+ * Prepare_MSOSM (msosm_prepare.h:19-40) and fft_block_size (msosm_gpu_batch.h:54). */
+int msosm_get_dims(const msosm_t *h, int *M, int *M_min, int *fftpoint, int *batch, int *num_dms,
+                   int *delaycount, int *ring_blocks);
+/* Nd_values (msosm_prepare.h:38), per-DM delaycount_values (:32). */
+int msosm_get_nd(const msosm_t *h, int *nd_out);
+int msosm_get_delaycounts(const msosm_t *h, int *dc_out);
+/* delay_points[dm] (msosm_prepare.h:36): 2M ints. */
+int msosm_get_delay_points(const msosm_t *h, int dm_index, int *out);
+/* dedisp_params[dm] (msosm_prepare.h:34): 2M complex64 as 4M floats. */
+int msosm_get_response(const msosm_t *h, int dm_index, float *out);
+
+/* One streaming step: B*M new samples of the init'ed format from `in` (host or
+ * device pointer; host memory should be pinned for an asynchronous copy), all
+ * DMs dedispersed, outputs and the attached fold updated.  Replaces
+ * MSOSM_GPU_BATCH::filter_block_uint16(uint16_pair*) (msosm_gpu_batch.h:20,
+ * msosm_gpu_batch.cpp:178-236) and its complex64 / int8 variants. */
+int msosm_process(msosm_t *h, const void *in, void *stream);
+/* `nsteps` consecutive steps from one contiguous input of nsteps*B*M samples. */
+int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *stream);
+
+/* Copy the last step's [D][B][M] output (format = the init'ed out_mode's series,
+ * complex64 if both) to `out` (host or device).  Replaces
+ * MSOSM_GPU_BATCH::get_output(uint16_pair*) (msosm_gpu_batch.h:21, .cpp:238-245). */
+int msosm_get_output(msosm_t *h, void *out, void *stream);
+/* Device pointer of the complex64 output, NULL unless MSOSM_OUT_C64.  Replaces
+ * get_output_pointer() (msosm_gpu_batch.h:24). */
+void *msosm_device_output(msosm_t *h);
+/* Device pointer of the uint16_pair output, NULL unless MSOSM_OUT_U16. */
+void *msosm_device_output_u16(msosm_t *h);
+/* Number of steps processed so far. */
+long long msosm_steps(const msosm_t *h);
+/* cudaStreamSynchronize(stream) (synchronize(), msosm_gpu_batch.cpp:247-250, used
+ * cudaDeviceSynchronize). */
+int msosm_sync(msosm_t *h, void *stream);
+/* Frees all device memory of the handle; never resets the device. */
+int msosm_destroy(msosm_t *h);
+const char *msosm_last_error(const msosm_t *h);
+
+/* ---- kernel timing ------------------------------------------------------------
+ * Takes the place of the reference's NVTX ranges "Convert and FFT", "Gather and
+ * Multiply", "IFFT", "Discard and Convert" (msosm_gpu_batch.cpp:206-243) with
+ * device-side numbers: when enabled, every kernel launch of the handle is
+ * bracketed by CUDA events on its own stream.  msosm_profile_read (after the
+ * stream is synchronised) returns, per kernel kind, the summed milliseconds,
+ * the launches, how many of them were timed, and the F-point transforms done.
+ * Launch and transform counts are kept even with timing off. */
+#define MSOSM_KERNEL_FWD_PASS1 0 /* decode + forward column transforms */
+#define MSOSM_KERNEL_FWD_PASS2 1 /* forward row transforms -> spectra ring */
+#define MSOSM_KERNEL_INV_PASS1 2 /* delayed-bin gather x response + inverse column transforms */
+#define MSOSM_KERNEL_INV_PASS2 3 /* inverse row transforms + discard/scale/encode/fold */
+int msosm_profile_enable(msosm_t *h, int on);
+int msosm_profile_reset(msosm_t *h);
+int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
+                       long long *transforms);
+
+/* ---- plain overlap-save (single DM) -----------------------------------------
+ * osm_create replaces Prepare_OSM(float bw, float dm, float f0) / OSM_GPU_BATCH
+ * (dedispersion/include/prepare.h:10, osm_gpu_batch.h:10): the filter order is
+ * M = 2*next_pow2(Nd) (osm_prepare.cpp:15-28) and every bin has delay 0, so the
+ * same engine runs it.  msosm_init then mirrors OSM_GPU_BATCH::initialize_uint16
+ * (osm_gpu_batch.cpp:19-92) and msosm_process its filter_block_uint16 (:94-123). */
+int osm_create(float bw, float dm, float f0, msosm_t **out);
+
+/* ---- folding -----------------------------------------------------------------
+ * msosm_fold_create replaces Fold_GPU(float period, float fs, unsigned long size,
+ *   string, unsigned long time_bin) (folding/include/fold_gpu.h:13,
+ *   fold_gpu.cpp:4-25) for `num_series` independent series (one per DM; the
+ *   reference folds one).  time_bin 0 means period*fs bins, like the reference's -1.
+ * msosm_fold_accumulate replaces calculate_intensity(pol1[, pol2]) followed by
+ *   fold_data_phase() (fold_gpu.cpp:27-54): pol1/pol2 are device complex64
+ *   series of num_series*size samples; pol2 NULL gives |a|^2, otherwise
+ *   sqrt(|a|^2+|b|^2) (gpu/gpu_kernel.cu:477-491); zero samples are skipped; the
+ *   fold's time origin advances by size/fs per call.
+ * msosm_fold_read replaces get_folded_data() (fold_gpu.cpp:56-60): folded mean
+ *   per bin (float, [num_series][time_bin]) and optionally the raw double sums
+ *   and counts.  Any output pointer may be NULL.
+ * msosm_attach_fold makes every msosm_process fold |x|^2 of each DM's new output
+ *   into row d inside the inverse transform (no series round trip through HBM).
+ *   The fold must have num_series == num_dms and size == B*M.
+ */
+int msosm_fold_create(float period, float fs, unsigned long size, unsigned long time_bin, int num_series,
+                      msosm_fold_t **out);
+int msosm_fold_accumulate(msosm_fold_t *f, const void *pol1, const void *pol2, void *stream);
+int msosm_fold_read(msosm_fold_t *f, float *folded, double *sums, unsigned long long *counts, void *stream);
+int msosm_fold_reset(msosm_fold_t *f, void *stream);
+int msosm_fold_dims(const msosm_fold_t *f, unsigned long *time_bin, int *num_series, unsigned long *size);
+int msosm_fold_destroy(msosm_fold_t *f);
+int msosm_attach_fold(msosm_t *h, msosm_fold_t *f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSOSM_GB300_H */
