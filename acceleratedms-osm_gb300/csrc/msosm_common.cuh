@@ -16,6 +16,8 @@ struct TileCfg
     static constexpr int THREADS = (POINTS / 16 < 32) ? 32 : (POINTS / 16);
     static constexpr int SMEM_DATA = TileGeom<N, COLS>::SMEM_ELEMS; // float2 elements
     static constexpr size_t SMEM_BYTES = (size_t)(SMEM_DATA + N) * sizeof(float2);
+    // two CTAs per SM: one CTA's loads overlap the other's butterflies
+    static constexpr int MIN_BLOCKS = 2;
 };
 
 // W_F^m from the two-level table: m = hi*N2 + lo.
@@ -56,13 +58,18 @@ __device__ __forceinline__ uint32_t encode_u16(float2 v)
 }
 
 // Add sample p (skipped when exactly zero, as foldDataPhase_kernel does) to
-// shared phase bin `bin`.  All 32 lanes must call it together.  A half-warp whose
-// 16 samples share one bin is reduced with shuffles and lands as one atomic.
+// shared phase bin `bin`.  All 32 lanes must call it together, and the samples of
+// each half-warp must be in time order spanning less than one period.  Bins are
+// then cyclically non-decreasing along the half-warp, so equal first and last
+// bins mean one shared bin: the half-warp is reduced with shuffles and lands as a
+// single atomic.
 __device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, unsigned bin, float p)
 {
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned half = (lane < 16u) ? 0x0000FFFFu : 0xFFFF0000u;
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, bin);
+    const unsigned base = lane & 16u;
+    const unsigned half = base ? 0xFFFF0000u : 0x0000FFFFu;
+    const unsigned b_first = __shfl_sync(0xFFFFFFFFu, bin, base);
+    const unsigned b_last = __shfl_sync(0xFFFFFFFFu, bin, base + 15u);
     const bool nz = (p != 0.0f);
     const unsigned nzmask = __ballot_sync(0xFFFFFFFFu, nz);
     float s = p;
@@ -70,7 +77,7 @@ __device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, u
     s += __shfl_xor_sync(0xFFFFFFFFu, s, 4);
     s += __shfl_xor_sync(0xFFFFFFFFu, s, 2);
     s += __shfl_xor_sync(0xFFFFFFFFu, s, 1);
-    if ((peers & half) == half)
+    if (b_first == b_last)
     {
         if ((lane & 15u) == 0u)
         {
@@ -95,12 +102,22 @@ __device__ __forceinline__ unsigned phase_bin(uint64_t ph, unsigned K)
     return (unsigned)__umul64hi(ph, (unsigned long long)K);
 }
 
+// Raise a kernel's dynamic shared-memory limit.  `granted` is the caller's
+// per-kernel cache (a function-local static in each launch wrapper, which is
+// instantiated once per kernel), indexed by device.
+constexpr int kMaxDevices = 64;
 template <class KERNEL>
-inline cudaError_t ensure_smem(KERNEL k, size_t bytes)
+inline cudaError_t ensure_smem(KERNEL k, size_t bytes, size_t (&granted)[kMaxDevices])
 {
-    if (bytes <= 48 * 1024)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        dev = 0;
+    if (bytes <= 48 * 1024 || bytes <= granted[dev])
         return cudaSuccess;
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess)
+        granted[dev] = bytes;
+    return e;
 }
 
 } // namespace msosm

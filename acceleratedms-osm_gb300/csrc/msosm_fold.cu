@@ -84,7 +84,8 @@ static cudaError_t fold_launch(const float2 *a, const float2 *b, size_t size, in
 {
     auto k = fold_kernel<TWO_POL, SMEM_BINS>;
     const size_t smem = SMEM_BINS ? (size_t)f.K * 8 : 0;
-    cudaError_t e = ensure_smem(k, smem);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
         return e;
     // ~4 chunks per SM across all series; each chunk a multiple of the block size

@@ -66,7 +66,7 @@ struct RingStore
 };
 
 template <int N, int FMT>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MIN_BLOCKS)
     fwd_pass1_kernel(const void *__restrict__ in, const float2 *__restrict__ tail, float2 *__restrict__ tail_next,
                      float2 *__restrict__ T, const float2 *__restrict__ twN2, const float2 *__restrict__ lo,
                      const float2 *__restrict__ hi, int B, int M, int N1, int n2_shift)
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(TileCfg<N>::THREADS)
 }
 
 template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MIN_BLOCKS)
     fwd_pass2_kernel(const float2 *__restrict__ T, float2 *__restrict__ ring, const float2 *__restrict__ twN1,
                      int rbi, int M, int N2)
 {
@@ -116,7 +116,8 @@ static cudaError_t fwd_pass1(const Geom &g, const Twiddles &tw, const void *in, 
 {
     using C = TileCfg<N>;
     auto k = fwd_pass1_kernel<N, FMT>;
-    cudaError_t e = ensure_smem(k, C::SMEM_BYTES);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, C::SMEM_BYTES, granted);
     if (e != cudaSuccess)
         return e;
     dim3 grid(g.N1 / C::COLS, B);
@@ -131,7 +132,8 @@ static cudaError_t fwd_pass2(const Geom &g, const Twiddles &tw, const float2 *T,
 {
     using C = TileCfg<N>;
     auto k = fwd_pass2_kernel<N>;
-    cudaError_t e = ensure_smem(k, C::SMEM_BYTES);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, C::SMEM_BYTES, granted);
     if (e != cudaSuccess)
         return e;
     dim3 grid(g.N2 / C::COLS, B);

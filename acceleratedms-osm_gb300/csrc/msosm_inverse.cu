@@ -91,7 +91,7 @@ struct InvEpilogue
 };
 
 template <int N>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MIN_BLOCKS)
     inv_pass1_kernel(const float2 *__restrict__ ring, const float2 *__restrict__ H, const uint16_t *__restrict__ delays,
                      float2 *__restrict__ T, const float2 *__restrict__ twN2, const float2 *__restrict__ lo,
                      const float2 *__restrict__ hi, long long g0, int B, int rbi, int fbs, int N1, int F,
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(TileCfg<N>::THREADS)
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(TileCfg<N>::THREADS)
+__global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MIN_BLOCKS)
     inv_pass2_kernel(const float2 *__restrict__ T, const float2 *__restrict__ twN1, long long g0, int B, int M,
                      int N2, float2 *__restrict__ out_c64, uint32_t *__restrict__ out_u16, FoldArgs fold)
 {
@@ -179,7 +179,8 @@ static cudaError_t inv_pass1(const Geom &g, const Twiddles &tw, const InvArgs &a
 {
     using C = TileCfg<N>;
     auto k = inv_pass1_kernel<N>;
-    cudaError_t e = ensure_smem(k, C::SMEM_BYTES);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, C::SMEM_BYTES, granted);
     if (e != cudaSuccess)
         return e;
     dim3 grid(g.N1 / C::COLS, count);
@@ -195,7 +196,8 @@ static cudaError_t inv_pass2_mode(const Geom &g, const Twiddles &tw, const InvAr
     using C = TileCfg<N>;
     auto k = inv_pass2_kernel<N, MODE>;
     const size_t smem = C::SMEM_BYTES + (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
-    cudaError_t e = ensure_smem(k, smem);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
         return e;
     dim3 grid(g.N2 / C::COLS, count);

@@ -335,6 +335,7 @@ def run_engine(args, w, rank, world, local):
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for _ in range(args.steps):
+        fold.reset(stream)  # each step folds exactly one pass over the baseband
         proc.filter_blocks(host, calls, stream)
         fold.read_folded(folded_host, stream)  # D2H of the step's result (synchronises)
     torch.cuda.synchronize()
@@ -382,10 +383,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_dm_512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--samples", type=int, default=0, help="override the baseband length (profiling captures)")
+    ap.add_argument("--dm-trials", type=int, default=0, help="override the DM-trial count (profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.samples:
+        w["samples"] = args.samples
+    if args.dm_trials:
+        w["n_dms"] = args.dm_trials
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, w, rank, world)
