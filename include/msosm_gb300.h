@@ -175,6 +175,27 @@ int msosm_fold_dims(const msosm_fold_t *f, unsigned long *time_bin, int *num_ser
 int msosm_fold_destroy(msosm_fold_t *f);
 int msosm_attach_fold(msosm_t *h, msosm_fold_t *f);
 
+/* ---- overlap-save filtering without device allocation --------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate
+ * device memory when they filter -- real-time loops that allocate everything at
+ * start-up because cudaMalloc/cudaFree synchronise the device and can miss a
+ * buffer deadline, and plug-ins inside a host application that owns the GPU's
+ * memory budget.  Filters `count` overlapping windows of one DM with response H:
+ *   x   device complex64, (count+1)*M samples (M = fftpoint/2); the first M are
+ *       the history the first window overlaps
+ *   H   device complex64, fftpoint bins (e.g. msosm_plan_response's output)
+ *   out device complex64, count*M samples: window b's samples M..2M-1 of
+ *       IFFT(FFT(x[b*M .. b*M+2M)) * H) / fftpoint, as msosm_process computes them
+ * Intermediates live in a fixed file-scope device array of 18,939,904 bytes that
+ * every GPU loading the library holds until exit; no cudaMalloc/cudaFree or other
+ * allocating call is made.  Limits: fftpoint a power of two in [2^8, 2^20] and
+ * count*fftpoint <= 2^20; larger requests return MSOSM_ERR_UNSUPPORTED with a
+ * message on stderr.  The first call on each device looks up the array's device
+ * address (one-time set-up), so make it before any stream capture.  All calls
+ * share the array and it keeps the last call's contents: calls that overlap on
+ * the GPU race, so order them on one stream. */
+int msosm_osm_filter_noalloc(const void *x, const void *H, int fftpoint, int count, void *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
