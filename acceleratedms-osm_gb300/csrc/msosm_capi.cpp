@@ -13,6 +13,7 @@
 #include "msosm_gb300.h"
 
 #include "msosm_kernels.cuh"
+#include "msosm_persist.cuh"
 #include "msosm_plan.h"
 
 #include <cuda_runtime.h>
@@ -35,6 +36,8 @@ constexpr int kMinLog2F = 8;
 constexpr int kMaxLog2F = 22;
 constexpr size_t kIntermediateBudget = 64ull << 20; // bytes of pass-1 output kept per launch pair
 constexpr unsigned kMaxFusedBins = 8192;
+constexpr int kMaxSlots = 64;                             // intermediate slots of the persistent transform
+constexpr unsigned long long kWaitTimeoutNs = 2000000000; // device-side wait limit (2 s)
 
 size_t in_elem_bytes(int fmt)
 {
@@ -90,12 +93,12 @@ void dfree(void *p)
 // transforms are counted whether or not timing is on.
 struct Profiler
 {
-    static constexpr int KINDS = 4;
+    static constexpr int KINDS = 5;
     bool on = false;
-    long long launches[KINDS] = {0, 0, 0, 0};
-    long long transforms[KINDS] = {0, 0, 0, 0};
-    double ms[KINDS] = {0, 0, 0, 0};
-    long long timed[KINDS] = {0, 0, 0, 0};
+    long long launches[KINDS] = {};
+    long long transforms[KINDS] = {};
+    double ms[KINDS] = {};
+    long long timed[KINDS] = {};
     struct Pending
     {
         int kind;
@@ -235,6 +238,12 @@ struct msosm_s
     uint32_t *d_out_u16 = nullptr;
     float2 *d_tw = nullptr;
     Twiddles tw_fwd{}, tw_inv{};
+    // persistent inverse transform (F >= 2^16): ticket + per-slot counters, error flag
+    bool persist = false;
+    int sms = 0;
+    int T_slots = 0;
+    unsigned *d_sync = nullptr; // [1 + 2*kMaxSlots]
+    int *d_err = nullptr;
     long long step = 0;
     msosm_fold_t *fold = nullptr;
     Profiler prof;
@@ -262,6 +271,10 @@ struct msosm_s
         dfree(d_out_c64);
         dfree(d_out_u16);
         dfree(d_tw);
+        dfree(d_sync);
+        dfree(d_err);
+        d_sync = nullptr;
+        d_err = nullptr;
         d_ring = d_H = d_T = d_out_c64 = d_tw = nullptr;
         d_tail[0] = d_tail[1] = nullptr;
         d_delays = nullptr;
@@ -521,7 +534,27 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
         return h->release(), h->cuda_fail(e, "cudaMemcpy(delays)");
     const long long per_launch = (long long)(kIntermediateBudget / ((size_t)F * sizeof(float2)));
     h->T_cap = (int)std::max<long long>(batch, std::min<long long>((long long)h->D * batch, std::max(1ll, per_launch)));
-    if ((e = dalloc(&h->d_T, (size_t)h->T_cap * F)) != cudaSuccess)
+    // persistent inverse transform: a few slots, enough for 2 CTAs per SM in flight
+    h->persist = msosm::persist_supported(L);
+    h->T_slots = h->T_cap;
+    if (h->persist)
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if ((e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaDeviceGetAttribute");
+        // at most 4 CTAs of 512 threads fit an SM, so at most 4*sms items are in flight
+        const int per_block = (int)(2 * F / 8192);
+        const int slots = std::min(kMaxSlots, (4 * h->sms + per_block - 1) / per_block + 4);
+        h->T_slots = std::max(batch, slots);
+        if ((e = dalloc(&h->d_sync, (size_t)1 + 2 * kMaxSlots)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMalloc(sync)");
+        if ((e = dalloc(&h->d_err, 1)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMalloc(err)");
+        if ((e = cudaMemset(h->d_err, 0, sizeof(int))) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaMemset(err)");
+    }
+    if ((e = dalloc(&h->d_T, (size_t)h->T_slots * F)) != cudaSuccess)
         return h->release(), h->cuda_fail(e, "cudaMalloc(intermediate)");
     for (int i = 0; i < 2; i++)
     {
@@ -676,7 +709,45 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         a.fold = h->fold->args();
     }
     const long long total = (long long)h->D * h->B;
-    for (long long g0 = 0; g0 < total; g0 += h->T_cap)
+    if (h->persist)
+    {
+        msosm::PersistArgs pa{};
+        pa.ring = h->d_ring;
+        pa.H = h->d_H;
+        pa.delays = h->d_delays;
+        pa.T = h->d_T;
+        pa.rbi = rbi;
+        pa.fbs = h->fbs;
+        pa.B = h->B;
+        pa.g0 = 0;
+        pa.G = total;
+        pa.tw = h->tw_inv;
+        pa.out_mode = a.out_mode;
+        pa.out_c64 = a.out_c64;
+        pa.out_u16 = a.out_u16;
+        pa.fold = a.fold;
+        pa.ticket = h->d_sync;
+        pa.p1_done = h->d_sync + 1;
+        pa.p2_done = h->d_sync + 1 + kMaxSlots;
+        pa.err = h->d_err;
+        pa.timeout_ns = kWaitTimeoutNs;
+        msosm::PersistPlan plan;
+        e = msosm::persist_plan(h->g.L, pa, h->sms, &plan);
+        if (e != cudaSuccess)
+            return h->cuda_fail(e, "persistent transform plan");
+        pa.lag = plan.lag;
+        pa.S = std::min(plan.slots, h->T_slots);
+        if (pa.S <= pa.lag)
+            return h->fail(MSOSM_ERR_UNSUPPORTED, "intermediate ring too small for the persistent transform");
+        if ((e = cudaMemsetAsync(h->d_sync, 0, sizeof(unsigned) * (1 + 2 * kMaxSlots), st)) != cudaSuccess)
+            return h->cuda_fail(e, "cudaMemsetAsync(sync)");
+        pr.begin(MSOSM_KERNEL_INV_FUSED, st);
+        e = msosm::launch_inverse_persistent(h->g.L, pa, h->sms, st);
+        pr.end(MSOSM_KERNEL_INV_FUSED, st, total);
+        if (e != cudaSuccess)
+            return h->cuda_fail(e, "persistent inverse transform launch");
+    }
+    for (long long g0 = 0; !h->persist && g0 < total; g0 += h->T_cap)
     {
         const int count = (int)std::min<long long>(h->T_cap, total - g0);
         pr.begin(MSOSM_KERNEL_INV_PASS1, st);
@@ -754,6 +825,16 @@ extern "C" int msosm_sync(msosm_t *h, void *stream)
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess)
         return h ? h->cuda_fail(e, "cudaStreamSynchronize") : MSOSM_ERR_CUDA;
+    if (h && h->d_err)
+    {
+        int err = 0;
+        e = cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            return h->cuda_fail(e, "cudaMemcpy(err)");
+        if (err)
+            return h->fail(MSOSM_ERR_CUDA, "a device-side wait of the persistent transform timed out; outputs of "
+                                           "this handle are invalid");
+    }
     return MSOSM_OK;
 }
 
@@ -823,7 +904,8 @@ extern "C" int msosm_fold_create(float period, float fs, unsigned long size, uns
     const float psf = period * fs;
     f->K = time_bin ? time_bin : (unsigned long)psf;
     f->S = num_series;
-    if (f->K == 0 || f->K > (1ul << 30))
+    // the fold kernels reduce runs of 16 consecutive samples (see fold_accumulate)
+    if (f->K == 0 || f->K > (1ul << 30) || (double)period * (double)fs <= 16.0)
     {
         delete f;
         return MSOSM_ERR_ARG;
@@ -938,6 +1020,15 @@ extern "C" int msosm_attach_fold(msosm_t *h, msosm_fold_t *f)
         return h->fail(MSOSM_ERR_ARG, "fold must have num_series == num_dms and size == B*M");
     if (f->K > kMaxFusedBins)
         return h->fail(MSOSM_ERR_UNSUPPORTED, "fused fold supports at most 8192 bins");
+    // The fused epilogue reduces each half-warp's 16 samples when their first and
+    // last bins agree, which needs those samples to span less than one period.
+    // A half-warp covers 16 consecutive time samples, or 16/cols runs of cols
+    // samples N2 apart when a tile holds fewer than 16 rows.
+    const int n1 = h->g.N1, n2 = h->g.N2;
+    const int cols = h->persist ? 8192 / n1 : (n1 <= 512 ? 16 : (n1 == 1024 ? 8 : 4));
+    const double span = cols >= 16 ? 16.0 : (double)(16 / cols - 1) * n2 + cols;
+    if ((double)f->P / f->dt <= span)
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "fold period shorter than the fused epilogue's sample span");
     h->fold = f;
     return MSOSM_OK;
 }

@@ -1,0 +1,352 @@
+// Persistent inverse transform: all (DM, window) transforms of one call in one
+// launch, the pass-1 -> pass-2 intermediate kept in a small ring of transform
+// slots that stays in L2.
+//
+// Work items, taken from a global ticket counter in this order:
+//   block q = 0 .. G+LAG-1 holds  [ P1(q, tile 0..n1t-1) | P2(q-LAG, tile 0..n2t-1) ]
+// P1(f, c): gather x response + N2-point column transforms of transform f,
+//           column tile c, into slot f mod S of the ring.
+// P2(f, r): N1-point row transforms of row tile r of transform f + the
+//           discard / encode / fold epilogue.
+// Dependencies, through per-slot completion counters (monotone over the launch):
+//   P2(f)  needs all P1(f)              : p1_done[f mod S] >= (f/S + 1) * n1t
+//   P1(f)  needs slot f mod S released  : p2_done[f mod S] >= (f/S) * n2t
+// Every item waited on holds a smaller ticket (S > LAG), and a CTA takes a new
+// ticket only after finishing its current item, so the smallest unfinished
+// ticket can always run: no deadlock whatever the residency.  Waits are
+// nevertheless bounded by %globaltimer; on timeout the kernel raises an error
+// flag, every later wait returns at once and the host reports the failure.
+#include "msosm_common.cuh"
+#include "msosm_persist.cuh"
+
+namespace msosm {
+
+namespace {
+
+constexpr int P_POINTS = 8192;
+constexpr int P_THREADS = 512;
+
+template <int N>
+struct PCfg
+{
+    static constexpr int COLS = P_POINTS / N;
+    static constexpr int LD = COLS + 1;
+    static constexpr int SMEM_DATA = N * LD;
+};
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread 0 waits until *cnt >= target (or the launch has failed); the CTA then
+// learns the outcome through shared memory.  Returns false if the item must be
+// skipped because the launch failed.
+__device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target, int *err, int *s_flag,
+                                           unsigned long long timeout_ns)
+{
+    if (threadIdx.x == 0)
+    {
+        int ok = 1;
+        if (ld_acquire(cnt) < target)
+        {
+            const uint64_t t0 = global_ns();
+            unsigned backoff = 32;
+            while (ld_acquire(cnt) < target)
+            {
+                if (*(volatile int *)err)
+                {
+                    ok = 0;
+                    break;
+                }
+                if (global_ns() - t0 > timeout_ns)
+                {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(backoff);
+                if (backoff < 1024)
+                    backoff *= 2;
+            }
+        }
+        *s_flag = ok;
+    }
+    __syncthreads();
+    const bool ok = *s_flag != 0;
+    __syncthreads();
+    return ok;
+}
+
+struct PInvLoader
+{
+    const float2 *ring;
+    const float2 *Hd;
+    const uint16_t *dl;
+    int c0, N1, F, fbs, rb;
+    __device__ __forceinline__ float2 load(int col, int n2) const
+    {
+        const int n = c0 + col + N1 * n2;
+        int slot = rb - (int)__ldg(dl + n);
+        if (slot < 0)
+            slot += fbs;
+        const float2 s = __ldcs(ring + (size_t)slot * F + n);
+        const float2 h = __ldg(Hd + n);
+        return cmul(s, h);
+    }
+};
+
+struct PStoreT
+{
+    float2 *T;
+    const float2 *lo, *hi;
+    int c0, N1;
+    unsigned n2_mask;
+    int n2_shift;
+    __device__ __forceinline__ void store(int col, int k2, float2 v) const
+    {
+        const int n1 = c0 + col;
+        const float2 w = twiddle_F(lo, hi, (unsigned)(n1 * k2), n2_mask, n2_shift);
+        T[n1 + (size_t)N1 * k2] = cmul(v, w);
+    }
+};
+
+struct PNoLoad
+{
+    __device__ __forceinline__ float2 load(int, int) const { return make_float2(0.f, 0.f); }
+};
+
+template <int MODE>
+struct PEpilogue
+{
+    float2 *out_c64;
+    uint32_t *out_u16;
+    float *s_sum;
+    unsigned *s_cnt;
+    uint64_t ph_b, dphase;
+    unsigned K;
+    int r0, N1, N2;
+    float scale;
+    __device__ __forceinline__ void store(int col, int k1, float2 v) const
+    {
+        if (k1 < (N1 >> 1))
+            return;
+        const int o = r0 + col + N2 * (k1 - (N1 >> 1));
+        v.x *= scale;
+        v.y *= scale;
+        if constexpr ((MODE & OUT_C64) != 0)
+            out_c64[o] = v;
+        if constexpr ((MODE & OUT_U16) != 0)
+            out_u16[o] = encode_u16(v);
+        if constexpr ((MODE & OUT_FOLD) != 0)
+        {
+            const float p = v.x * v.x + v.y * v.y;
+            fold_accumulate(s_sum, s_cnt, phase_bin(ph_b + (uint64_t)o * dphase, K), p);
+        }
+    }
+};
+
+template <int N1, int N2, int MODE>
+__global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArgs a)
+{
+    using C1 = PCfg<N2>; // pass 1: columns of length N2
+    using C2 = PCfg<N1>; // pass 2: rows of length N1
+    constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
+    constexpr int n1t = N1 / C1::COLS; // P1 items per transform
+    constexpr int n2t = N2 / C2::COLS; // P2 items per transform
+    constexpr int per_block = n1t + n2t;
+    constexpr int F = N1 * N2;
+    constexpr int M = F / 2;
+    extern __shared__ float2 smem[];
+    float2 *sm = smem;
+    float2 *tw1 = smem + DATA; // W_{N2}: pass-1 stages
+    float2 *tw2 = tw1 + N2;    // W_{N1}: pass-2 stages
+    float *s_sum = reinterpret_cast<float *>(tw2 + N1);
+    unsigned *s_cnt = reinterpret_cast<unsigned *>(s_sum + (((MODE & OUT_FOLD) != 0) ? a.fold.K : 0));
+    __shared__ unsigned s_ticket;
+    __shared__ int s_flag;
+
+    for (int i = threadIdx.x; i < N2; i += P_THREADS)
+        tw1[i] = __ldg(a.tw.twN2 + i);
+    for (int i = threadIdx.x; i < N1; i += P_THREADS)
+        tw2[i] = __ldg(a.tw.twN1 + i);
+
+    const long long total = (a.G + a.lag) * (long long)per_block;
+    const int B = a.B;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_ticket = atomicAdd(a.ticket, 1u);
+        __syncthreads(); // also fences the previous item's shared-memory use
+        const long long t = s_ticket;
+        if (t >= total)
+            break;
+        const long long q = t / per_block;
+        const int w = (int)(t % per_block);
+        const bool is_p1 = w < n1t;
+        const long long f = is_p1 ? q : q - a.lag;
+        if (f < 0 || f >= a.G)
+            continue;
+        const int slot = (int)(f % a.S);
+        const unsigned gen = (unsigned)(f / a.S);
+        float2 *Ts = a.T + (size_t)slot * F;
+        const long long gi = a.g0 + f;
+        const int d = (int)(gi / B), b = (int)(gi % B);
+        if (is_p1)
+        {
+            if (!wait_count(a.p2_done + slot, gen * n2t, a.err, &s_flag, a.timeout_ns))
+                continue;
+            const int c0 = w * C1::COLS;
+            PInvLoader ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs, a.rbi + b};
+            PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N1, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
+            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true>(sm, tw1, ld, st);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                atomicAdd(a.p1_done + slot, 1u);
+        }
+        else
+        {
+            if (!wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, &s_flag, a.timeout_ns))
+                continue;
+            const int r0 = (w - n1t) * C2::COLS;
+            const float2 *src = Ts + (size_t)r0 * N1;
+#pragma unroll 4
+            for (int e = threadIdx.x; e < P_POINTS; e += P_THREADS)
+            {
+                const int col = e / N1, n = e % N1;
+                sm[n * C2::LD + col] = __ldcg(src + e);
+            }
+            if constexpr ((MODE & OUT_FOLD) != 0)
+            {
+                for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
+                {
+                    s_sum[i] = 0.0f;
+                    s_cnt[i] = 0u;
+                }
+            }
+            __syncthreads();
+            // the slot may be refilled as soon as every thread holds its data
+            if (threadIdx.x == 0)
+                atomicAdd(a.p2_done + slot, 1u);
+            const size_t row = ((size_t)d * B + b) * M;
+            PEpilogue<MODE> ep{a.out_c64 ? a.out_c64 + row : nullptr,
+                               a.out_u16 ? a.out_u16 + row : nullptr,
+                               s_sum,
+                               s_cnt,
+                               a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
+                               a.fold.dphase,
+                               a.fold.K,
+                               r0,
+                               N1,
+                               N2,
+                               1.0f / (float)F};
+            fft_stages<N1, C2::COLS, P_THREADS, +1, 1, false>(sm, tw2, PNoLoad{}, ep);
+            if constexpr ((MODE & OUT_FOLD) != 0)
+            {
+                __syncthreads();
+                double *gs = a.fold.sum + (size_t)d * a.fold.K;
+                unsigned long long *gc = a.fold.cnt + (size_t)d * a.fold.K;
+                for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
+                {
+                    const unsigned c = s_cnt[i];
+                    if (c)
+                    {
+                        atomicAdd(gs + i, (double)s_sum[i]);
+                        atomicAdd(gc + i, (unsigned long long)c);
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int N1, int N2, int MODE>
+cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    using C1 = PCfg<N2>;
+    using C2 = PCfg<N1>;
+    constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
+    auto k = inv_persistent_kernel<N1, N2, MODE>;
+    const size_t smem = (size_t)(DATA + N1 + N2) * sizeof(float2) +
+                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
+    static size_t granted[kMaxDevices] = {};
+    cudaError_t e = ensure_smem(k, smem, granted);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P_THREADS, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    const int grid = per_sm * sms;
+    constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
+    if (plan)
+    {
+        // enough look-behind that items in flight rarely wait; slots > LAG
+        plan->lag = (grid + per_block - 1) / per_block + 2;
+        plan->slots = plan->lag + 2;
+        plan->grid = grid;
+        return cudaSuccess;
+    }
+    if (a.S <= a.lag)
+        return cudaErrorInvalidValue;
+    k<<<grid, P_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int N1, int N2>
+cudaError_t persist_mode(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    switch (a.out_mode)
+    {
+    case OUT_C64: return persist_launch<N1, N2, OUT_C64>(a, sms, st, plan);
+    case OUT_U16: return persist_launch<N1, N2, OUT_U16>(a, sms, st, plan);
+    case OUT_FOLD: return persist_launch<N1, N2, OUT_FOLD>(a, sms, st, plan);
+    case OUT_C64 | OUT_FOLD: return persist_launch<N1, N2, OUT_C64 | OUT_FOLD>(a, sms, st, plan);
+    case OUT_U16 | OUT_FOLD: return persist_launch<N1, N2, OUT_U16 | OUT_FOLD>(a, sms, st, plan);
+    case OUT_C64 | OUT_U16: return persist_launch<N1, N2, OUT_C64 | OUT_U16>(a, sms, st, plan);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t persist_dispatch(int L, const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    switch (L)
+    {
+    case 16: return persist_mode<256, 256>(a, sms, st, plan);
+    case 17: return persist_mode<256, 512>(a, sms, st, plan);
+    case 18: return persist_mode<512, 512>(a, sms, st, plan);
+    case 19: return persist_mode<512, 1024>(a, sms, st, plan);
+    case 20: return persist_mode<1024, 1024>(a, sms, st, plan);
+    case 21: return persist_mode<1024, 2048>(a, sms, st, plan);
+    case 22: return persist_mode<2048, 2048>(a, sms, st, plan);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace
+
+bool persist_supported(int L) { return L >= 16 && L <= 22; }
+
+cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan)
+{
+    return persist_dispatch(L, a, sms, nullptr, plan);
+}
+
+cudaError_t launch_inverse_persistent(int L, const PersistArgs &a, int sms, cudaStream_t st)
+{
+    return persist_dispatch(L, a, sms, st, nullptr);
+}
+
+} // namespace msosm

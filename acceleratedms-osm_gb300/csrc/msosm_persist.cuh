@@ -1,0 +1,38 @@
+// Persistent inverse transform (see msosm_persist.cu).
+#pragma once
+#include "msosm_kernels.cuh"
+
+namespace msosm {
+
+struct PersistArgs
+{
+    const float2 *ring;
+    const float2 *H;
+    const uint16_t *delays;
+    float2 *T;       // S slots of F complex values
+    int S, lag;      // ring slots of T and the P2 look-behind in transforms
+    int rbi, fbs, B;
+    long long g0, G; // transforms g0 .. g0+G-1 (g = d*B + b)
+    Twiddles tw;     // inverse direction
+    int out_mode;
+    float2 *out_c64;
+    uint32_t *out_u16;
+    FoldArgs fold;
+    unsigned *ticket;  // zeroed before the launch
+    unsigned *p1_done; // [S], zeroed before the launch
+    unsigned *p2_done; // [S], zeroed before the launch
+    int *err;          // sticky error flag (1 = a wait timed out)
+    unsigned long long timeout_ns;
+};
+
+struct PersistPlan
+{
+    int lag = 0, slots = 0, grid = 0;
+};
+
+bool persist_supported(int L);
+// Grid and ring geometry for the given sizes / output mode (no launch).
+cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan);
+cudaError_t launch_inverse_persistent(int L, const PersistArgs &a, int sms, cudaStream_t st);
+
+} // namespace msosm

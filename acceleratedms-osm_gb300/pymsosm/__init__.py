@@ -222,7 +222,7 @@ class MsosmGpuBatch:
         self._fold = fold
 
     # -- kernel timing ------------------------------------------------------
-    KERNELS = ("fwd_pass1", "fwd_pass2", "inv_pass1", "inv_pass2")
+    KERNELS = ("fwd_pass1", "fwd_pass2", "inv_pass1", "inv_pass2", "inv_persistent")
 
     def profile(self, on: bool = True):
         self._check(lib().msosm_profile_enable(self._h, 1 if on else 0))

@@ -136,6 +136,7 @@ const char *msosm_last_error(const msosm_t *h);
 #define MSOSM_KERNEL_FWD_PASS2 1 /* forward row transforms -> spectra ring */
 #define MSOSM_KERNEL_INV_PASS1 2 /* delayed-bin gather x response + inverse column transforms */
 #define MSOSM_KERNEL_INV_PASS2 3 /* inverse row transforms + discard/scale/encode/fold */
+#define MSOSM_KERNEL_INV_FUSED 4 /* both inverse passes in one persistent launch (F >= 2^16) */
 int msosm_profile_enable(msosm_t *h, int on);
 int msosm_profile_reset(msosm_t *h);
 int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
