@@ -108,6 +108,19 @@ struct TileGeom
     static constexpr int SMEM_ELEMS = N * LD;
 };
 
+// A destination may take a butterfly's R outputs at once (store_group<R, Ns>)
+// instead of one at a time, e.g. to derive per-output factors by recurrence.
+template <class T, class = void>
+struct HasStoreGroup
+{
+    static constexpr bool value = false;
+};
+template <class T>
+struct HasStoreGroup<T, decltype((void)&T::template store_group<2, 1>, void())>
+{
+    static constexpr bool value = true;
+};
+
 // Shared-memory source/destination for a stage.
 template <int N, int COLS>
 struct SmemIO
@@ -160,9 +173,14 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
         const int j = beta / COLS;
         const int k = j & (Ns - 1);
         const int base = (j / Ns) * Ns * R + k;
+        if constexpr (HasStoreGroup<DST>::value)
+            dst.template store_group<R, Ns>(col, base, v[i]); // outputs base + r*Ns, r = 0..R-1
+        else
+        {
 #pragma unroll
-        for (int r = 0; r < R; r++)
-            dst.store(col, base + r * Ns, v[i][r]);
+            for (int r = 0; r < R; r++)
+                dst.store(col, base + r * Ns, v[i][r]);
+        }
     }
     if constexpr (DST_SMEM)
         __syncthreads();

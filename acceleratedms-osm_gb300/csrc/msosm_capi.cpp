@@ -36,7 +36,7 @@ constexpr int kMinLog2F = 8;
 constexpr int kMaxLog2F = 22;
 constexpr size_t kIntermediateBudget = 64ull << 20; // bytes of pass-1 output kept per launch pair
 constexpr unsigned kMaxFusedBins = 8192;
-constexpr int kMaxSlots = 64;                             // intermediate slots of the persistent transform
+constexpr int kMaxSlots = 256;                            // intermediate slots of the persistent transform
 constexpr unsigned long long kWaitTimeoutNs = 2000000000; // device-side wait limit (2 s)
 
 size_t in_elem_bytes(int fmt)
@@ -543,9 +543,11 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
         cudaGetDevice(&dev);
         if ((e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
             return h->release(), h->cuda_fail(e, "cudaDeviceGetAttribute");
-        // at most 4 CTAs of 512 threads fit an SM, so at most 4*sms items are in flight
+        // at most 4 CTAs of 512 threads fit an SM, each holding two tickets; the
+        // kernel plans lag = 2*ceil(grid/items per transform) + 2 and 2*lag slots
         const int per_block = (int)(2 * F / 8192);
-        const int slots = std::min(kMaxSlots, (4 * h->sms + per_block - 1) / per_block + 4);
+        const int lag_max = 2 * ((4 * h->sms + per_block - 1) / per_block) + 2;
+        const int slots = std::min(kMaxSlots, 2 * lag_max);
         h->T_slots = std::max(batch, slots);
         if ((e = dalloc(&h->d_sync, (size_t)1 + 2 * kMaxSlots)) != cudaSuccess)
             return h->release(), h->cuda_fail(e, "cudaMalloc(sync)");

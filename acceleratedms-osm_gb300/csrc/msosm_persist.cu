@@ -48,43 +48,36 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
     return v;
 }
 
-// Thread 0 waits until *cnt >= target (or the launch has failed); the CTA then
-// learns the outcome through shared memory.  Returns false if the item must be
-// skipped because the launch failed.
-__device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target, int *err, int *s_flag,
+// Called by one thread: wait until *cnt >= target.  False if the launch failed
+// meanwhile (another CTA raised the error flag) or this wait timed out (raises it).
+// Polls with volatile loads (served by L2, no L1 invalidation), then one
+// acquire load orders the caller's later reads after the observed count.
+__device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target, int *err,
                                            unsigned long long timeout_ns)
 {
-    if (threadIdx.x == 0)
+    const volatile unsigned *vc = cnt;
+    if (*vc >= target)
     {
-        int ok = 1;
-        if (ld_acquire(cnt) < target)
-        {
-            const uint64_t t0 = global_ns();
-            unsigned backoff = 32;
-            while (ld_acquire(cnt) < target)
-            {
-                if (*(volatile int *)err)
-                {
-                    ok = 0;
-                    break;
-                }
-                if (global_ns() - t0 > timeout_ns)
-                {
-                    atomicExch(err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(backoff);
-                if (backoff < 1024)
-                    backoff *= 2;
-            }
-        }
-        *s_flag = ok;
+        (void)ld_acquire(cnt);
+        return true;
     }
-    __syncthreads();
-    const bool ok = *s_flag != 0;
-    __syncthreads();
-    return ok;
+    const uint64_t t0 = global_ns();
+    unsigned backoff = 32;
+    while (*vc < target)
+    {
+        if (*(volatile int *)err)
+            return false;
+        if (global_ns() - t0 > timeout_ns)
+        {
+            atomicExch(err, 1);
+            return false;
+        }
+        __nanosleep(backoff);
+        if (backoff < 1024)
+            backoff *= 2;
+    }
+    (void)ld_acquire(cnt);
+    return true;
 }
 
 struct PInvLoader
@@ -117,6 +110,22 @@ struct PStoreT
         const int n1 = c0 + col;
         const float2 w = twiddle_F(lo, hi, (unsigned)(n1 * k2), n2_mask, n2_shift);
         T[n1 + (size_t)N1 * k2] = cmul(v, w);
+    }
+    // Last stage: outputs k2 = base + r*Ns.  W_F^(n1*k2) = W_F^(n1*base) * (W_F^(n1*Ns))^r,
+    // two table lookups per butterfly and a product chain instead of two per output.
+    template <int R, int Ns>
+    __device__ __forceinline__ void store_group(int col, int base, const float2 *v) const
+    {
+        const int n1 = c0 + col;
+        float2 w = twiddle_F(lo, hi, (unsigned)(n1 * base), n2_mask, n2_shift);
+        const float2 step = twiddle_F(lo, hi, (unsigned)(n1 * Ns), n2_mask, n2_shift);
+        float2 *dst = T + n1 + (size_t)N1 * base;
+#pragma unroll
+        for (int r = 0; r < R; r++)
+        {
+            dst[(size_t)N1 * Ns * r] = cmul(v[r], w);
+            w = cmul(w, step);
+        }
     }
 };
 
@@ -172,8 +181,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     float2 *tw2 = tw1 + N2;    // W_{N1}: pass-2 stages
     float *s_sum = reinterpret_cast<float *>(tw2 + N1);
     unsigned *s_cnt = reinterpret_cast<unsigned *>(s_sum + (((MODE & OUT_FOLD) != 0) ? a.fold.K : 0));
-    __shared__ unsigned s_ticket;
-    __shared__ int s_flag;
+    // (ticket, verdict) published by thread 0; double-buffered by iteration parity
+    // so a skipped item (no barrier inside) cannot overwrite what slow threads read
+    __shared__ unsigned s_ticket[2];
+    __shared__ int s_verdict[2];
 
     for (int i = threadIdx.x; i < N2; i += P_THREADS)
         tw1[i] = __ldg(a.tw.twN2 + i);
@@ -182,29 +193,53 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
 
     const long long total = (a.G + a.lag) * (long long)per_block;
     const int B = a.B;
-    for (;;)
+    unsigned held = 0; // thread 0: the ticket of the next item, fetched one item ahead
+    if (threadIdx.x == 0)
+        held = atomicAdd(a.ticket, 1u);
+    for (unsigned it = 0;; it++)
     {
+        const int par = it & 1;
         if (threadIdx.x == 0)
-            s_ticket = atomicAdd(a.ticket, 1u);
+        {
+            const unsigned t = held;
+            int verdict = -1; // -1 stop, 0 skip, 1 run
+            if ((long long)t < total)
+            {
+                held = atomicAdd(a.ticket, 1u); // its latency overlaps this item
+                const long long q = t / per_block;
+                const int w = (int)(t % per_block);
+                const bool p1 = w < n1t;
+                const long long f = p1 ? q : q - a.lag;
+                verdict = 0;
+                if (f >= 0 && f < a.G)
+                {
+                    const int slot = (int)(f % a.S);
+                    const unsigned gen = (unsigned)(f / a.S);
+                    const bool ok = p1 ? wait_count(a.p2_done + slot, gen * n2t, a.err, a.timeout_ns)
+                                       : wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, a.timeout_ns);
+                    verdict = ok ? 1 : 0;
+                }
+            }
+            s_ticket[par] = t;
+            s_verdict[par] = verdict;
+        }
         __syncthreads(); // also fences the previous item's shared-memory use
-        const long long t = s_ticket;
-        if (t >= total)
+        const int verdict = s_verdict[par];
+        if (verdict < 0)
             break;
+        if (verdict == 0)
+            continue;
+        const long long t = s_ticket[par];
         const long long q = t / per_block;
         const int w = (int)(t % per_block);
         const bool is_p1 = w < n1t;
         const long long f = is_p1 ? q : q - a.lag;
-        if (f < 0 || f >= a.G)
-            continue;
         const int slot = (int)(f % a.S);
-        const unsigned gen = (unsigned)(f / a.S);
         float2 *Ts = a.T + (size_t)slot * F;
         const long long gi = a.g0 + f;
         const int d = (int)(gi / B), b = (int)(gi % B);
         if (is_p1)
         {
-            if (!wait_count(a.p2_done + slot, gen * n2t, a.err, &s_flag, a.timeout_ns))
-                continue;
             const int c0 = w * C1::COLS;
             PInvLoader ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs, a.rbi + b};
             PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N1, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
@@ -216,8 +251,6 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         }
         else
         {
-            if (!wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, &s_flag, a.timeout_ns))
-                continue;
             const int r0 = (w - n1t) * C2::COLS;
             const float2 *src = Ts + (size_t)r0 * N1;
 #pragma unroll 4
@@ -293,9 +326,12 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
     if (plan)
     {
-        // enough look-behind that items in flight rarely wait; slots > LAG
-        plan->lag = (grid + per_block - 1) / per_block + 2;
-        plan->slots = plan->lag + 2;
+        // Enough look-behind that items in flight rarely wait: every CTA holds its
+        // current ticket and the next one.  P2(f) sits LAG blocks after P1(f); a
+        // slot is reused S blocks later, so P1(f) waits on P2(f-S), S-LAG blocks
+        // back: S = 2*LAG keeps both distances at LAG.
+        plan->lag = 2 * ((grid + per_block - 1) / per_block) + 2;
+        plan->slots = 2 * plan->lag;
         plan->grid = grid;
         return cudaSuccess;
     }
