@@ -134,35 +134,95 @@ struct PNoLoad
     __device__ __forceinline__ float2 load(int, int) const { return make_float2(0.f, 0.f); }
 };
 
-template <int MODE>
+// Last pass-2 stage: outputs k1 = base + r*Ns of row (r0 + col); only k1 >= N1/2
+// (window samples M..2M-1) survive, i.e. r >= R/2.  Series outputs go straight to
+// global memory; for the fold, |v|^2 is parked in a shared tile s_p[(k1 - N1/2)*COLS
+// + col], in time order, for fold_tile() to bin.
+template <int MODE, int COLS>
 struct PEpilogue
 {
     float2 *out_c64;
     uint32_t *out_u16;
-    float *s_sum;
-    unsigned *s_cnt;
-    uint64_t ph_b, dphase;
-    unsigned K;
+    float *s_p;
     int r0, N1, N2;
     float scale;
-    __device__ __forceinline__ void store(int col, int k1, float2 v) const
+    template <int R, int Ns>
+    __device__ __forceinline__ void store_group(int col, int base, const float2 *v) const
     {
-        if (k1 < (N1 >> 1))
-            return;
-        const int o = r0 + col + N2 * (k1 - (N1 >> 1));
-        v.x *= scale;
-        v.y *= scale;
-        if constexpr ((MODE & OUT_C64) != 0)
-            out_c64[o] = v;
-        if constexpr ((MODE & OUT_U16) != 0)
-            out_u16[o] = encode_u16(v);
-        if constexpr ((MODE & OUT_FOLD) != 0)
+#pragma unroll
+        for (int r = R / 2; r < R; r++)
         {
-            const float p = v.x * v.x + v.y * v.y;
-            fold_accumulate(s_sum, s_cnt, phase_bin(ph_b + (uint64_t)o * dphase, K), p);
+            const int k1h = base + r * Ns - (N1 >> 1);
+            float2 x = v[r];
+            x.x *= scale;
+            x.y *= scale;
+            const int o = r0 + col + N2 * k1h;
+            if constexpr ((MODE & OUT_C64) != 0)
+                out_c64[o] = x;
+            if constexpr ((MODE & OUT_U16) != 0)
+                out_u16[o] = encode_u16(x);
+            if constexpr ((MODE & OUT_FOLD) != 0)
+                s_p[k1h * COLS + col] = x.x * x.x + x.y * x.y;
         }
     }
 };
+
+// Bin the staged tile: each thread takes runs of G consecutive time samples; a
+// run whose first and last samples share a phase bin (runs are far shorter than a
+// period, and phase is monotone within a run) is summed in registers and lands as
+// one shared atomic; other runs go sample by sample.  Zero samples are skipped as
+// foldDataPhase_kernel does.
+template <int COLS, int HALF>
+__device__ __forceinline__ void fold_tile(const float *s_p, float *s_sum, unsigned *s_cnt, uint64_t ph_b,
+                                          uint64_t dphase, unsigned K, int r0, int N2)
+{
+    constexpr int SAMPLES = COLS * HALF;
+    constexpr int PER_T = SAMPLES / P_THREADS;
+    constexpr int G = PER_T < COLS ? PER_T : COLS;
+    static_assert(SAMPLES % P_THREADS == 0 && PER_T % G == 0, "fold tile shape");
+#pragma unroll
+    for (int g0 = 0; g0 < PER_T; g0 += G)
+    {
+        const int e0 = threadIdx.x * PER_T + g0;
+        const int k1h = e0 / COLS, c = e0 % COLS;
+        const uint64_t ph0 = ph_b + (uint64_t)(r0 + c + N2 * k1h) * dphase;
+        const unsigned bf = phase_bin(ph0, K);
+        const unsigned bl = phase_bin(ph0 + (uint64_t)(G - 1) * dphase, K);
+        float p[G];
+#pragma unroll
+        for (int i = 0; i < G; i++)
+            p[i] = s_p[e0 + i];
+        if (bf == bl)
+        {
+            float s = 0.0f;
+            unsigned n = 0;
+#pragma unroll
+            for (int i = 0; i < G; i++)
+            {
+                s += p[i];
+                n += (p[i] != 0.0f);
+            }
+            if (n)
+            {
+                atomicAdd(s_sum + bf, s);
+                atomicAdd(s_cnt + bf, n);
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < G; i++)
+            {
+                if (p[i] != 0.0f)
+                {
+                    const unsigned bi = phase_bin(ph0 + (uint64_t)i * dphase, K);
+                    atomicAdd(s_sum + bi, p[i]);
+                    atomicAdd(s_cnt + bi, 1u);
+                }
+            }
+        }
+    }
+}
 
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArgs a)
@@ -179,7 +239,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     float2 *sm = smem;
     float2 *tw1 = smem + DATA; // W_{N2}: pass-1 stages
     float2 *tw2 = tw1 + N2;    // W_{N1}: pass-2 stages
-    float *s_sum = reinterpret_cast<float *>(tw2 + N1);
+    float *s_p = reinterpret_cast<float *>(tw2 + N1); // fold staging tile (C2::COLS * N1/2 floats)
+    float *s_sum = s_p + (((MODE & OUT_FOLD) != 0) ? C2::COLS * (N1 / 2) : 0);
     unsigned *s_cnt = reinterpret_cast<unsigned *>(s_sum + (((MODE & OUT_FOLD) != 0) ? a.fold.K : 0));
     // (ticket, verdict) published by thread 0; double-buffered by iteration parity
     // so a skipped item (no barrier inside) cannot overwrite what slow threads read
@@ -272,20 +333,20 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             if (threadIdx.x == 0)
                 atomicAdd(a.p2_done + slot, 1u);
             const size_t row = ((size_t)d * B + b) * M;
-            PEpilogue<MODE> ep{a.out_c64 ? a.out_c64 + row : nullptr,
-                               a.out_u16 ? a.out_u16 + row : nullptr,
-                               s_sum,
-                               s_cnt,
-                               a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
-                               a.fold.dphase,
-                               a.fold.K,
-                               r0,
-                               N1,
-                               N2,
-                               1.0f / (float)F};
+            PEpilogue<MODE, C2::COLS> ep{a.out_c64 ? a.out_c64 + row : nullptr,
+                                         a.out_u16 ? a.out_u16 + row : nullptr,
+                                         s_p,
+                                         r0,
+                                         N1,
+                                         N2,
+                                         1.0f / (float)F};
             fft_stages<N1, C2::COLS, P_THREADS, +1, 1, false>(sm, tw2, PNoLoad{}, ep);
             if constexpr ((MODE & OUT_FOLD) != 0)
             {
+                __syncthreads();
+                fold_tile<C2::COLS, N1 / 2>(s_p, s_sum, s_cnt,
+                                            a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
+                                            a.fold.dphase, a.fold.K, r0, N2);
                 __syncthreads();
                 double *gs = a.fold.sum + (size_t)d * a.fold.K;
                 unsigned long long *gc = a.fold.cnt + (size_t)d * a.fold.K;
@@ -311,7 +372,7 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
     auto k = inv_persistent_kernel<N1, N2, MODE>;
     const size_t smem = (size_t)(DATA + N1 + N2) * sizeof(float2) +
-                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
+                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 + (size_t)C2::COLS * (N1 / 2) * 4 : 0);
     static size_t granted[kMaxDevices] = {};
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
