@@ -885,6 +885,183 @@ extern "C" int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long l
     return MSOSM_OK;
 }
 
+// ---- DM derivative ------------------------------------------------------------------
+extern "C" int msosm_plan_response_derivative(float bw, float f0, float dm, int M, float *H_out)
+{
+    if (M <= 0 || !is_pow2(M) || !H_out)
+        return MSOSM_ERR_ARG;
+    msosm::plan_responses(bw, f0, &dm, 1, M, H_out, 1, true);
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_use_response_derivative(msosm_t *h)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "use_response_derivative before init");
+    const size_t DF = (size_t)h->D * h->F;
+    std::vector<float> H(2 * DF);
+    const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    msosm::plan_responses(h->bw, h->f0, h->dms.data(), h->D, h->M, H.data(), threads, true);
+    cudaError_t e = cudaMemcpy(h->d_H, H.data(), DF * sizeof(float2), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? MSOSM_OK : h->cuda_fail(e, "cudaMemcpy(dH)");
+}
+
+extern "C" int msosm_fold_accumulate_cross(msosm_fold_t *f, const void *x, const void *dx, void *stream)
+{
+    if (!f || !x || !dx)
+        return MSOSM_ERR_ARG;
+    cudaError_t e = msosm::launch_fold((const float2 *)x, (const float2 *)dx, f->size, f->S, f->args(),
+                                       (cudaStream_t)stream, msosm::FOLD_CROSS);
+    if (e != cudaSuccess)
+    {
+        f->err = std::string("fold launch: ") + cudaGetErrorString(e);
+        return MSOSM_ERR_CUDA;
+    }
+    f->t_start += (double)f->size * f->dt;
+    return MSOSM_OK;
+}
+
+// ---- checkpoint / resume --------------------------------------------------------
+namespace {
+struct StreamStateHeader
+{
+    uint32_t magic; // 'MSST'
+    uint32_t version;
+    int32_t M, F, B, fbs, in_format, tail_cur;
+    int64_t step;
+};
+constexpr uint32_t kStateMagic = 0x5453534Du;
+struct FoldStateHeader
+{
+    uint32_t magic; // 'MSFS'
+    uint32_t version;
+    uint64_t K, size;
+    int32_t S, pad;
+    double t_start, P, dt;
+};
+constexpr uint32_t kFoldMagic = 0x5346534Du;
+} // namespace
+
+extern "C" size_t msosm_state_bytes(const msosm_t *h)
+{
+    if (!h || !h->inited)
+        return 0;
+    return sizeof(StreamStateHeader) + ((size_t)h->M + (size_t)h->fbs * h->F) * sizeof(float2);
+}
+
+extern "C" int msosm_save_state(msosm_t *h, void *buf, size_t bytes, void *stream)
+{
+    if (!h || !buf)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "save_state before init");
+    if (bytes < msosm_state_bytes(h))
+        return h->fail(MSOSM_ERR_ARG, "state buffer too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    StreamStateHeader hd{kStateMagic, 1, h->M, h->F, h->B, h->fbs, h->in_format, h->tail_cur, h->step};
+    char *p = static_cast<char *>(buf);
+    cudaError_t e = cudaMemcpyAsync(p, &hd, sizeof(hd), cudaMemcpyDefault, st);
+    p += sizeof(hd);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p, h->d_tail[h->tail_cur], (size_t)h->M * sizeof(float2), cudaMemcpyDefault, st);
+    p += (size_t)h->M * sizeof(float2);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p, h->d_ring, (size_t)h->fbs * h->F * sizeof(float2), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? MSOSM_OK : h->cuda_fail(e, "save_state");
+}
+
+extern "C" int msosm_load_state(msosm_t *h, const void *buf, size_t bytes, void *stream)
+{
+    if (!h || !buf)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "load_state before init");
+    if (bytes < msosm_state_bytes(h))
+        return h->fail(MSOSM_ERR_ARG, "state buffer too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    StreamStateHeader hd{};
+    cudaError_t e = cudaMemcpyAsync(&hd, buf, sizeof(hd), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "load_state");
+    if (hd.magic != kStateMagic || hd.version != 1)
+        return h->fail(MSOSM_ERR_ARG, "not a stream state");
+    if (hd.M != h->M || hd.F != h->F || hd.B != h->B || hd.fbs != h->fbs)
+        return h->fail(MSOSM_ERR_ARG, "state was saved with a different M, batch or ring size");
+    const char *p = static_cast<const char *>(buf) + sizeof(hd);
+    // the saved tail becomes the current tail buffer
+    e = cudaMemcpyAsync(h->d_tail[h->tail_cur], p, (size_t)h->M * sizeof(float2), cudaMemcpyDefault, st);
+    p += (size_t)h->M * sizeof(float2);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_ring, p, (size_t)h->fbs * h->F * sizeof(float2), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "load_state");
+    h->step = hd.step;
+    return MSOSM_OK;
+}
+
+extern "C" size_t msosm_fold_state_bytes(const msosm_fold_t *f)
+{
+    if (!f)
+        return 0;
+    return sizeof(FoldStateHeader) + (size_t)f->K * f->S * (sizeof(double) + sizeof(unsigned long long));
+}
+
+extern "C" int msosm_fold_save_state(msosm_fold_t *f, void *buf, size_t bytes, void *stream)
+{
+    if (!f || !buf || bytes < msosm_fold_state_bytes(f))
+        return MSOSM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)f->K * f->S;
+    FoldStateHeader hd{kFoldMagic, 1, f->K, f->size, f->S, 0, f->t_start, f->P, f->dt};
+    char *p = static_cast<char *>(buf);
+    cudaError_t e = cudaMemcpyAsync(p, &hd, sizeof(hd), cudaMemcpyDefault, st);
+    p += sizeof(hd);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p, f->d_sum, n * sizeof(double), cudaMemcpyDefault, st);
+    p += n * sizeof(double);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p, f->d_cnt, n * sizeof(unsigned long long), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? MSOSM_OK : MSOSM_ERR_CUDA;
+}
+
+extern "C" int msosm_fold_load_state(msosm_fold_t *f, const void *buf, size_t bytes, void *stream)
+{
+    if (!f || !buf || bytes < msosm_fold_state_bytes(f))
+        return MSOSM_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    FoldStateHeader hd{};
+    cudaError_t e = cudaMemcpyAsync(&hd, buf, sizeof(hd), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return MSOSM_ERR_CUDA;
+    if (hd.magic != kFoldMagic || hd.version != 1 || hd.K != f->K || hd.S != f->S || hd.size != f->size ||
+        hd.P != f->P || hd.dt != f->dt)
+        return MSOSM_ERR_ARG;
+    const size_t n = (size_t)f->K * f->S;
+    const char *p = static_cast<const char *>(buf) + sizeof(hd);
+    e = cudaMemcpyAsync(f->d_sum, p, n * sizeof(double), cudaMemcpyDefault, st);
+    p += n * sizeof(double);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(f->d_cnt, p, n * sizeof(unsigned long long), cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return MSOSM_ERR_CUDA;
+    f->t_start = hd.t_start;
+    return MSOSM_OK;
+}
+
 // ---- folding ------------------------------------------------------------------
 extern "C" int msosm_fold_create(float period, float fs, unsigned long size, unsigned long time_bin, int num_series,
                                  msosm_fold_t **out)

@@ -63,14 +63,14 @@ __device__ __forceinline__ uint32_t encode_u16(float2 v)
 // then cyclically non-decreasing along the half-warp, so equal first and last
 // bins mean one shared bin: the half-warp is reduced with shuffles and lands as a
 // single atomic.
-__device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, unsigned bin, float p)
+// `nz` says whether the sample counts (p may be a signed term that is zero).
+__device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, unsigned bin, float p, bool nz)
 {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned base = lane & 16u;
     const unsigned half = base ? 0xFFFF0000u : 0x0000FFFFu;
     const unsigned b_first = __shfl_sync(0xFFFFFFFFu, bin, base);
     const unsigned b_last = __shfl_sync(0xFFFFFFFFu, bin, base + 15u);
-    const bool nz = (p != 0.0f);
     const unsigned nzmask = __ballot_sync(0xFFFFFFFFu, nz);
     float s = p;
     s += __shfl_xor_sync(0xFFFFFFFFu, s, 8);
@@ -94,6 +94,11 @@ __device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, u
         atomicAdd(s_sum + bin, p);
         atomicAdd(s_cnt + bin, 1u);
     }
+}
+
+__device__ __forceinline__ void fold_accumulate(float *s_sum, unsigned *s_cnt, unsigned bin, float p)
+{
+    fold_accumulate(s_sum, s_cnt, bin, p, p != 0.0f);
 }
 
 // Phase bin of a Q0.64 phase: floor(phase * K).

@@ -14,7 +14,7 @@ namespace msosm {
 constexpr int FOLD_THREADS = 256;
 constexpr unsigned FOLD_SMEM_MAX_BINS = 12288; // 96 KB of bins
 
-template <bool TWO_POL, bool SMEM_BINS>
+template <int KIND, bool SMEM_BINS>
 __global__ void __launch_bounds__(FOLD_THREADS)
     fold_kernel(const float2 *__restrict__ a, const float2 *__restrict__ b, size_t size, FoldArgs f, size_t chunk)
 {
@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(FOLD_THREADS)
     unsigned *s_cnt = reinterpret_cast<unsigned *>(fsm + (SMEM_BINS ? f.K : 0));
     const int s = blockIdx.y;
     const float2 *pa = a + (size_t)s * size;
-    const float2 *pb = TWO_POL ? b + (size_t)s * size : nullptr;
+    const float2 *pb = KIND != FOLD_POWER ? b + (size_t)s * size : nullptr;
     if constexpr (SMEM_BINS)
     {
         for (unsigned i = threadIdx.x; i < f.K; i += FOLD_THREADS)
@@ -40,22 +40,34 @@ __global__ void __launch_bounds__(FOLD_THREADS)
     {
         const size_t i = base + threadIdx.x;
         float p = 0.0f;
+        bool nz = false;
         unsigned bin = 0;
         if (i < end)
         {
             const float2 x = __ldcs(pa + i);
-            if constexpr (TWO_POL)
+            if constexpr (KIND == FOLD_POWER2)
             {
                 const float2 y = __ldcs(pb + i);
                 p = sqrtf(x.x * x.x + x.y * x.y + y.x * y.x + y.y * y.y);
+                nz = p != 0.0f;
+            }
+            else if constexpr (KIND == FOLD_CROSS)
+            {
+                // 2 Re(conj(a) b), counted where |a|^2 is, so counts match the power fold
+                const float2 y = __ldcs(pb + i);
+                p = 2.0f * (x.x * y.x + x.y * y.y);
+                nz = (x.x * x.x + x.y * x.y) != 0.0f;
             }
             else
+            {
                 p = x.x * x.x + x.y * x.y;
+                nz = p != 0.0f;
+            }
             bin = phase_bin(f.phase0 + (uint64_t)i * f.dphase, f.K);
         }
         if constexpr (SMEM_BINS)
-            fold_accumulate(s_sum, s_cnt, bin, p);
-        else if (p != 0.0f)
+            fold_accumulate(s_sum, s_cnt, bin, p, nz);
+        else if (nz)
         {
             atomicAdd(f.sum + (size_t)s * f.K + bin, (double)p);
             atomicAdd(f.cnt + (size_t)s * f.K + bin, 1ULL);
@@ -78,11 +90,11 @@ __global__ void __launch_bounds__(FOLD_THREADS)
     }
 }
 
-template <bool TWO_POL, bool SMEM_BINS>
+template <int KIND, bool SMEM_BINS>
 static cudaError_t fold_launch(const float2 *a, const float2 *b, size_t size, int series, const FoldArgs &f,
                                cudaStream_t st)
 {
-    auto k = fold_kernel<TWO_POL, SMEM_BINS>;
+    auto k = fold_kernel<KIND, SMEM_BINS>;
     const size_t smem = SMEM_BINS ? (size_t)f.K * 8 : 0;
     static size_t granted[kMaxDevices] = {};
     cudaError_t e = ensure_smem(k, smem, granted);
@@ -101,17 +113,24 @@ static cudaError_t fold_launch(const float2 *a, const float2 *b, size_t size, in
     return cudaGetLastError();
 }
 
+template <int KIND>
+static cudaError_t fold_kind(const float2 *pol1, const float2 *pol2, size_t size, int series, const FoldArgs &f,
+                             cudaStream_t st)
+{
+    return f.K <= FOLD_SMEM_MAX_BINS ? fold_launch<KIND, true>(pol1, pol2, size, series, f, st)
+                                     : fold_launch<KIND, false>(pol1, pol2, size, series, f, st);
+}
+
 cudaError_t launch_fold(const float2 *pol1, const float2 *pol2, size_t size, int series, const FoldArgs &f,
-                        cudaStream_t st)
+                        cudaStream_t st, int kind /* = FOLD_POWER */)
 {
     if (size == 0 || series <= 0)
         return cudaSuccess;
-    const bool smem_bins = f.K <= FOLD_SMEM_MAX_BINS;
+    if (kind == FOLD_CROSS)
+        return fold_kind<FOLD_CROSS>(pol1, pol2, size, series, f, st);
     if (pol2)
-        return smem_bins ? fold_launch<true, true>(pol1, pol2, size, series, f, st)
-                         : fold_launch<true, false>(pol1, pol2, size, series, f, st);
-    return smem_bins ? fold_launch<false, true>(pol1, nullptr, size, series, f, st)
-                     : fold_launch<false, false>(pol1, nullptr, size, series, f, st);
+        return fold_kind<FOLD_POWER2>(pol1, pol2, size, series, f, st);
+    return fold_kind<FOLD_POWER>(pol1, nullptr, size, series, f, st);
 }
 
 __global__ void fold_finalize_kernel(const double *__restrict__ sum, const unsigned long long *__restrict__ cnt,

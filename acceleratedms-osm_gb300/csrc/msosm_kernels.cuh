@@ -71,10 +71,18 @@ cudaError_t launch_inverse_p2(const Geom &g, const Twiddles &tw, const InvArgs &
                               cudaStream_t st);
 
 // Standalone intensity + phase fold of `size` samples of one or two complex series
-// (Fold_GPU::calculate_intensity + fold_data_phase).  pol2 == nullptr: |a|^2, else
-// sqrt(|a|^2+|b|^2).  series: number of consecutive series of length `size`.
+// (Fold_GPU::calculate_intensity + fold_data_phase).  kind FOLD_POWER: pol2 ==
+// nullptr gives |a|^2, otherwise sqrt(|a|^2+|b|^2) (FOLD_POWER2); FOLD_CROSS folds
+// 2 Re(conj(a) b), counted where |a|^2 != 0 (the derivative of |a|^2 when b = da).
+// series: number of consecutive series of length `size`.
+enum FoldKind : int
+{
+    FOLD_POWER = 0,
+    FOLD_POWER2 = 1,
+    FOLD_CROSS = 2,
+};
 cudaError_t launch_fold(const float2 *pol1, const float2 *pol2, size_t size, int series, const FoldArgs &f,
-                        cudaStream_t st);
+                        cudaStream_t st, int kind = FOLD_POWER);
 
 // folded[i] = cnt ? sum/cnt : 0 (computeFoldedData_kernel)
 cudaError_t launch_fold_finalize(const double *sum, const unsigned long long *cnt, float *folded, size_t n,

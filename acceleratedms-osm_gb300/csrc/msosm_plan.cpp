@@ -152,7 +152,10 @@ std::vector<cd> make_table(int n)
 //   H[2k]   = c[k]                                (FFT_M undoes IFFT_M)
 //   H[2k+1] = FFT_M(h[j] * exp(-i pi j / M))[k],  h = IFFT_M(c)/M
 // which needs two M-point transforms instead of an M- and a 2M-point one.
-void response_into(float bw, float f0, float dm, int M, float *Hout, const cd *tw, const cd *twist, cd *c, cd *h)
+// derivative == true gives dH/dDM: the chirp's phase is linear in DM, so
+// d/dDM exp(-i phi) = -i (phi/DM) exp(-i phi), and the construction is linear.
+void response_into(float bw, float f0, float dm, int M, float *Hout, const cd *tw, const cd *twist, cd *c, cd *h,
+                   bool derivative)
 {
     const double kdm_d = 4.15e15;
     const double fs_d = (double)bw, dm_d = (double)dm, f0_d = (double)f0;
@@ -164,6 +167,11 @@ void response_into(float bw, float f0, float dm, int M, float *Hout, const cd *t
         const double phase = 4.0 * kPi * kPi * kdm_d * dm_d * w * w / ((w + w0_d) * w0_d * w0_d);
         const int dst = (j < M / 2) ? (M / 2 + j) : (j - M / 2);
         c[dst] = cd(std::cos(phase), -std::sin(phase));
+        if (derivative)
+        {
+            const double per_dm = 4.0 * kPi * kPi * kdm_d * w * w / ((w + w0_d) * w0_d * w0_d);
+            c[dst] *= cd(0.0, -per_dm);
+        }
     }
     std::memcpy((void *)h, (const void *)c, sizeof(cd) * (size_t)M);
     fft_inplace(h, M, +1, tw);
@@ -198,7 +206,7 @@ void plan_response(float bw, float f0, float dm, int M, float *Hout)
     plan_responses(bw, f0, &dm, 1, M, Hout, 1);
 }
 
-void plan_responses(float bw, float f0, const float *dms, int n, int M, float *Hout, int threads)
+void plan_responses(float bw, float f0, const float *dms, int n, int M, float *Hout, int threads, bool derivative)
 {
     if (n <= 0)
         return;
@@ -208,7 +216,8 @@ void plan_responses(float bw, float f0, const float *dms, int n, int M, float *H
     auto work = [&](int t) {
         std::vector<cd> c(M), h(M);
         for (int i = t; i < n; i += nt)
-            response_into(bw, f0, dms[i], M, Hout + (size_t)i * 4 * M, tw.data(), twist.data(), c.data(), h.data());
+            response_into(bw, f0, dms[i], M, Hout + (size_t)i * 4 * M, tw.data(), twist.data(), c.data(), h.data(),
+                          derivative);
     };
     if (nt == 1)
     {

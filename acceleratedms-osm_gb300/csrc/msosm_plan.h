@@ -26,7 +26,9 @@ int plan_segmentation(float bw, float f0, float dm, int nd, int M, uint16_t *del
 // generate_dedisp_params(i) (msosm_prepare.cpp:107-164), FP64 throughout, rounded
 // to complex64 at the end.  Hout: 2M interleaved (re, im) floats.
 void plan_response(float bw, float f0, float dm, int M, float *Hout);
-// Responses of many DMs on up to `threads` host threads.
-void plan_responses(float bw, float f0, const float *dms, int n, int M, float *Hout, int threads);
+// Responses of many DMs on up to `threads` host threads; with derivative set,
+// dH/dDM instead (same construction applied to -i (phi/DM) exp(-i phi)).
+void plan_responses(float bw, float f0, const float *dms, int n, int M, float *Hout, int threads,
+                    bool derivative = false);
 
 } // namespace msosm

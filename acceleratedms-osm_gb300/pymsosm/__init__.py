@@ -101,6 +101,17 @@ def _declare(L):
     L.msosm_profile_enable.argtypes = [P, I]
     L.msosm_profile_reset.argtypes = [P]
     L.msosm_profile_read.argtypes = [P, I, C.POINTER(D), C.POINTER(LL), C.POINTER(LL), C.POINTER(LL)]
+    L.msosm_state_bytes.restype = C.c_size_t
+    L.msosm_state_bytes.argtypes = [P]
+    L.msosm_save_state.argtypes = [P, P, C.c_size_t, P]
+    L.msosm_load_state.argtypes = [P, P, C.c_size_t, P]
+    L.msosm_fold_state_bytes.restype = C.c_size_t
+    L.msosm_fold_state_bytes.argtypes = [P]
+    L.msosm_fold_save_state.argtypes = [P, P, C.c_size_t, P]
+    L.msosm_fold_load_state.argtypes = [P, P, C.c_size_t, P]
+    L.msosm_plan_response_derivative.argtypes = [F, F, F, I, P]
+    L.msosm_use_response_derivative.argtypes = [P]
+    L.msosm_fold_accumulate_cross.argtypes = [P, P, P, P]
     L.msosm_plan_nd.argtypes = [F, F, P, I, P]
     L.msosm_plan_min_order.argtypes = [P, I, P]
     L.msosm_plan_segmentation.argtypes = [F, F, F, I, I, P, P]
@@ -136,6 +147,13 @@ def plan_response(bw, f0, dm, M) -> np.ndarray:
     H = np.zeros(2 * M, np.complex64)
     if lib().msosm_plan_response(bw, f0, dm, M, H.ctypes.data) != OK:
         raise MsosmError("msosm_plan_response")
+    return H
+
+
+def plan_response_derivative(bw, f0, dm, M) -> np.ndarray:
+    H = np.zeros(2 * M, np.complex64)
+    if lib().msosm_plan_response_derivative(bw, f0, dm, M, H.ctypes.data) != OK:
+        raise MsosmError("msosm_plan_response_derivative")
     return H
 
 
@@ -220,6 +238,20 @@ class MsosmGpuBatch:
     def attach_fold(self, fold: "FoldGpu | None"):
         self._check(lib().msosm_attach_fold(self._h, fold._h if fold is not None else None))
         self._fold = fold
+
+    # -- checkpoint / derivative -------------------------------------------
+    def save_state(self, stream=None) -> np.ndarray:
+        n = lib().msosm_state_bytes(self._h)
+        buf = np.zeros(n, np.uint8)
+        self._check(lib().msosm_save_state(self._h, buf.ctypes.data, n, _stream(stream)))
+        return buf
+
+    def load_state(self, buf: np.ndarray, stream=None):
+        self._check(lib().msosm_load_state(self._h, buf.ctypes.data, buf.nbytes, _stream(stream)))
+
+    def use_response_derivative(self):
+        """Outputs become dx/dDM (responses replaced by dH/dDM, delays unchanged)."""
+        self._check(lib().msosm_use_response_derivative(self._h))
 
     # -- kernel timing ------------------------------------------------------
     KERNELS = ("fwd_pass1", "fwd_pass2", "inv_pass1", "inv_pass2", "inv_persistent")
@@ -316,6 +348,23 @@ class FoldGpu:
         if rc != OK:
             raise MsosmError(f"fold read: {lib().msosm_status_string(rc).decode()}")
         return folded, sums, cnts
+
+    def accumulate_cross(self, x, dx, stream=None):
+        """Fold 2 Re(conj(x) dx) (counted where |x|^2 != 0)."""
+        rc = lib().msosm_fold_accumulate_cross(self._h, _ptr(x), _ptr(dx), _stream(stream))
+        if rc != OK:
+            raise MsosmError(f"fold accumulate_cross: {lib().msosm_status_string(rc).decode()}")
+
+    def save_state(self, stream=None) -> np.ndarray:
+        n = lib().msosm_fold_state_bytes(self._h)
+        buf = np.zeros(n, np.uint8)
+        if lib().msosm_fold_save_state(self._h, buf.ctypes.data, n, _stream(stream)) != OK:
+            raise MsosmError("fold save_state")
+        return buf
+
+    def load_state(self, buf: np.ndarray, stream=None):
+        if lib().msosm_fold_load_state(self._h, buf.ctypes.data, buf.nbytes, _stream(stream)) != OK:
+            raise MsosmError("fold load_state")
 
     def read_folded(self, out: np.ndarray, stream=None):
         """Folded means only, into a caller-owned float32 [num_series][time_bin] array."""

@@ -142,6 +142,37 @@ int msosm_profile_reset(msosm_t *h);
 int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
                        long long *transforms);
 
+/* ---- DM derivative ---------------------------------------------------------------
+ * No counterpart in the reference.  With the segmentation (integer block delays)
+ * held fixed, the dedispersed series depends on DM only through the response,
+ * and the chirp phase is linear in DM, so dx/dDM is the same pipeline run with
+ * dH/dDM in place of H.  For folded-profile sharpness S = sum_k P_k^2, with
+ * P_k = sum|x|^2 / n_k:  dS/dDM = sum_k 2 P_k * (sum 2 Re(conj(x) dx/dDM)) / n_k.
+ * msosm_plan_response_derivative  dH/dDM for one DM (2M complex64, FP64 inside)
+ * msosm_use_response_derivative   replace a handle's responses by dH/dDM, so its
+ *                                 outputs are dx/dDM for the same input
+ * msosm_fold_accumulate_cross     fold 2 Re(conj(x) dx) (x, dx: device complex64,
+ *                                 num_series*size samples), counting the samples
+ *                                 where |x|^2 != 0, as the power fold counts them */
+int msosm_plan_response_derivative(float bw, float f0, float dm, int M, float *H_out);
+int msosm_use_response_derivative(msosm_t *h);
+int msosm_fold_accumulate_cross(msosm_fold_t *f, const void *x, const void *dx, void *stream);
+
+/* ---- checkpoint / resume -------------------------------------------------------
+ * No counterpart in the reference (its stream state lives only in device memory,
+ * msosm_gpu_batch.cpp:146-148, 218-221).  The state of a stream is the previous
+ * call's last M samples, the ring of past spectra and the call counter; it does
+ * not depend on the DM list, so it can be restored into any handle with the same
+ * M, batch and ring size.  msosm_state_bytes gives the buffer size; save/load copy
+ * through a host (or device) buffer and synchronise `stream`.  The fold's state
+ * (double sums, counts, time origin) is saved separately. */
+size_t msosm_state_bytes(const msosm_t *h);
+int msosm_save_state(msosm_t *h, void *buf, size_t bytes, void *stream);
+int msosm_load_state(msosm_t *h, const void *buf, size_t bytes, void *stream);
+size_t msosm_fold_state_bytes(const msosm_fold_t *f);
+int msosm_fold_save_state(msosm_fold_t *f, void *buf, size_t bytes, void *stream);
+int msosm_fold_load_state(msosm_fold_t *f, const void *buf, size_t bytes, void *stream);
+
 /* ---- plain overlap-save (single DM) -----------------------------------------
  * osm_create replaces Prepare_OSM(float bw, float dm, float f0) / OSM_GPU_BATCH
  * (dedispersion/include/prepare.h:10, osm_gpu_batch.h:10): the filter order is

@@ -290,6 +290,40 @@ void orc_response(float bw, float f0, float dm, int M, double *H)
     orc64_fft(H, F, -1, 1);
 }
 
+/* dH/dDM of the response above (no counterpart in the reference): the chirp
+ * phase is linear in DM, so d/dDM exp(-i phi) = -i (phi/DM) exp(-i phi); the
+ * IFFT_M / zero-pad / FFT_2M construction is linear and is applied unchanged. */
+void orc_response_derivative(float bw, float f0, float dm, int M, double *H)
+{
+    const double pi_d = ORC_PI;
+    const double kdm_d = 4.15e15;
+    const double fs_d = (double)bw;
+    const double dm_d = (double)dm;
+    const double w0_d = 2.0 * pi_d * (double)f0;
+    const double step = 2.0 * pi_d * fs_d / (double)M;
+    const int F = 2 * M;
+    double *h = (double *)malloc(sizeof(double) * 2 * (size_t)M);
+    for (int j = 0; j < M; j++)
+    {
+        double w = step * (double)j;
+        double per_dm = 4.0 * pi_d * pi_d * kdm_d * w * w / ((w + w0_d) * w0_d * w0_d);
+        double phase = per_dm * dm_d;
+        int dst = (j < M / 2) ? (M / 2 + j) : (j - M / 2);
+        /* -i * per_dm * (cos - i sin) = -per_dm * sin - i per_dm * cos */
+        h[2 * dst] = -per_dm * sin(phase);
+        h[2 * dst + 1] = -per_dm * cos(phase);
+    }
+    orc64_fft(h, M, +1, 1);
+    memset(H, 0, sizeof(double) * 2 * (size_t)F);
+    for (int j = 0; j < M; j++)
+    {
+        H[2 * j] = h[2 * j] / (double)M;
+        H[2 * j + 1] = h[2 * j + 1] / (double)M;
+    }
+    free(h);
+    orc64_fft(H, F, -1, 1);
+}
+
 /* Prepare_OSM::calculate_min_order, osm_prepare.cpp:15-28: M = 2*next_pow2((int)Nd) */
 unsigned long orc_osm_min_order(unsigned long nd)
 {

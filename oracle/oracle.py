@@ -85,6 +85,8 @@ def _declare(L):
     L.orc_build_segments.argtypes = [P, I, I, P, P, P]
     L.orc_response.restype = None
     L.orc_response.argtypes = [F, F, F, I, P]
+    L.orc_response_derivative.restype = None
+    L.orc_response_derivative.argtypes = [F, F, F, I, P]
     L.orc_osm_min_order.restype = UL
     L.orc_osm_min_order.argtypes = [UL]
     L.orc_decode_u16.argtypes = [P, SZ, P]
@@ -153,6 +155,13 @@ def build_segments(delay: np.ndarray, maxlen: int = 256):
 def response(bw, f0, dm, M) -> np.ndarray:
     H = np.zeros(2 * M, dtype=np.complex128)
     lib().orc_response(bw, f0, dm, M, _p(H))
+    return H
+
+
+def response_derivative(bw, f0, dm, M) -> np.ndarray:
+    """dH/dDM (FP64), for the gradient checks."""
+    H = np.zeros(2 * M, dtype=np.complex128)
+    lib().orc_response_derivative(bw, f0, dm, M, _p(H))
     return H
 
 
