@@ -24,7 +24,7 @@ INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["msosm_forward.cu", "msosm_inverse.cu", "msosm_persist.cu", "msosm_fold.cu", "msosm_noalloc.cu"]
-CPP_SOURCES = ["msosm_plan.cpp", "msosm_capi.cpp"]
+CPP_SOURCES = ["msosm_plan.cpp", "msosm_capi.cpp", "msosm_writer.cpp"]
 
 
 def _nvcc() -> str:

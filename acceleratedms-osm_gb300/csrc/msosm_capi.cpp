@@ -15,6 +15,7 @@
 #include "msosm_kernels.cuh"
 #include "msosm_persist.cuh"
 #include "msosm_plan.h"
+#include "msosm_writer.h"
 
 #include <cuda_runtime.h>
 
@@ -246,6 +247,7 @@ struct msosm_s
     int *d_err = nullptr;
     long long step = 0;
     msosm_fold_t *fold = nullptr;
+    msosm_writer_s *writer = nullptr;
     Profiler prof;
     std::string err;
 
@@ -765,8 +767,33 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     }
     if (h->fold)
         h->fold->t_start += (double)((size_t)h->B * h->M) * h->fold->dt; // fold_gpu.cpp:96
+    if (h->writer)
+    {
+        std::string werr;
+        int rc = msosm::writer_submit_device(h->writer, h->d_out_u16, st, werr);
+        if (rc != MSOSM_OK)
+            return h->fail(rc, werr);
+    }
     h->tail_cur ^= 1;
     h->step++;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_attach_writer(msosm_t *h, msosm_writer_t *w)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (!w)
+    {
+        h->writer = nullptr;
+        return MSOSM_OK;
+    }
+    if (!h->inited || !h->d_out_u16)
+        return h->fail(MSOSM_ERR_STATE, "attach_writer needs an initialised handle with MSOSM_OUT_U16");
+    if (msosm::writer_num_files(w) != h->D ||
+        msosm::writer_bytes_per_step(w) != (size_t)h->D * h->B * h->M * sizeof(uint32_t))
+        return h->fail(MSOSM_ERR_ARG, "writer must have one file per DM and B*M*4 bytes per DM per step");
+    h->writer = w;
     return MSOSM_OK;
 }
 

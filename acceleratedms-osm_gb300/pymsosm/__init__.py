@@ -112,6 +112,14 @@ def _declare(L):
     L.msosm_plan_response_derivative.argtypes = [F, F, F, I, P]
     L.msosm_use_response_derivative.argtypes = [P]
     L.msosm_fold_accumulate_cross.argtypes = [P, P, P, P]
+    L.msosm_writer_create.argtypes = [C.c_char_p, C.c_char_p, P, I, C.c_ulonglong, I, I, C.POINTER(P)]
+    L.msosm_attach_writer.argtypes = [P, P]
+    L.msosm_writer_write.argtypes = [P, P]
+    L.msosm_writer_join.argtypes = [P]
+    L.msosm_writer_last_error.restype = C.c_char_p
+    L.msosm_writer_last_error.argtypes = [P]
+    L.msosm_writer_filename.argtypes = [P, I, C.c_char_p, C.c_size_t]
+    L.msosm_writer_destroy.argtypes = [P]
     L.msosm_plan_nd.argtypes = [F, F, P, I, P]
     L.msosm_plan_min_order.argtypes = [P, I, P]
     L.msosm_plan_segmentation.argtypes = [F, F, F, I, I, P, P]
@@ -387,3 +395,61 @@ class FoldGpu:
             self.close()
         except Exception:
             pass
+
+
+class Writer:
+    """Per-DM output files (MSOSM_DataSave_Uring without liburing)."""
+
+    def __init__(self, directory: str, prefix: str, dms, bytes_per_dm: int, slots: int = 4, direct_io: bool = False):
+        L = lib()
+        d = np.ascontiguousarray(np.atleast_1d(np.asarray(dms, np.float32)))
+        self._h = P()
+        rc = L.msosm_writer_create(str(directory).encode(), prefix.encode(), d.ctypes.data, len(d), bytes_per_dm,
+                                   slots, 1 if direct_io else 0, C.byref(self._h))
+        if rc != OK:
+            raise MsosmError(f"writer create: {L.msosm_status_string(rc).decode()}")
+        self.num_dms, self.bytes_per_dm = len(d), bytes_per_dm
+
+    def filenames(self) -> list[str]:
+        out = []
+        for i in range(self.num_dms):
+            buf = C.create_string_buffer(4096)
+            lib().msosm_writer_filename(self._h, i, buf, 4096)
+            out.append(buf.value.decode())
+        return out
+
+    def write(self, block: np.ndarray):
+        assert block.nbytes == self.num_dms * self.bytes_per_dm
+        if lib().msosm_writer_write(self._h, np.ascontiguousarray(block).ctypes.data) != OK:
+            raise MsosmError("writer write")
+
+    def join(self):
+        rc = lib().msosm_writer_join(self._h)
+        if rc != OK:
+            raise MsosmError(f"writer: {lib().msosm_writer_last_error(self._h).decode()}")
+
+    def attach_to(self, m: MsosmGpuBatch):
+        m._check(lib().msosm_attach_writer(m._h, self._h))
+        m._writer = self
+
+    def close(self):
+        if self._h:
+            lib().msosm_writer_destroy(self._h)
+            self._h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def read_dat(path) -> np.ndarray:
+    """A per-DM .dat file as complex64: uint32 words, low 16 bits real, high 16
+    imaginary, value - 32768 unless the code is 0 (python_check/check.py:5-53)."""
+    w = np.fromfile(path, dtype=np.uint32)
+    re = (w & 0xFFFF).astype(np.int64)
+    im = (w >> 16).astype(np.int64)
+    re = np.where(re != 0, re - 32768, 0)
+    im = np.where(im != 0, im - 32768, 0)
+    return (re + 1j * im).astype(np.complex64)

@@ -142,6 +142,31 @@ int msosm_profile_reset(msosm_t *h);
 int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
                        long long *transforms);
 
+/* ---- per-DM output files -------------------------------------------------------
+ * Replaces MSOSM_DataSave_Uring (data_save/include/msosm_data_save_uring.h:22-52,
+ * msosm_data_save_uring.cpp:40-288) with pwrite worker threads (no liburing):
+ * msosm_writer_create  config_save + initialize_uring: one file per DM,
+ *                      <dir>/<prefix>_DM<value>.dat (decimals chosen as the reference
+ *                      does), `slots` page-aligned host buffers of num_dms*bytes_per_dm
+ *                      (pinned when a GPU is present); direct_io asks for O_DIRECT
+ *                      (used when the file system accepts it)
+ * msosm_attach_writer  after every msosm_process the handle's uint16 output (B*M
+ *                      pairs per DM; the handle must have MSOSM_OUT_U16) is copied
+ *                      into a free slot on the call's stream and written at offset
+ *                      step*bytes_per_dm of each DM's file (copy_to_slot +
+ *                      save_to_disk); blocks while every slot is busy
+ * msosm_writer_write   the same from a host block [num_dms][bytes_per_dm]
+ * msosm_writer_join    join_saving: wait for all writes; the first I/O or CUDA error */
+typedef struct msosm_writer_s msosm_writer_t;
+int msosm_writer_create(const char *dir, const char *prefix, const float *dms, int num_dms,
+                        unsigned long long bytes_per_dm, int slots, int direct_io, msosm_writer_t **out);
+int msosm_attach_writer(msosm_t *h, msosm_writer_t *w);
+int msosm_writer_write(msosm_writer_t *w, const void *host_block);
+int msosm_writer_join(msosm_writer_t *w);
+const char *msosm_writer_last_error(const msosm_writer_t *w);
+int msosm_writer_filename(const msosm_writer_t *w, int dm_index, char *buf, size_t len);
+int msosm_writer_destroy(msosm_writer_t *w);
+
 /* ---- DM derivative ---------------------------------------------------------------
  * No counterpart in the reference.  With the segmentation (integer block delays)
  * held fixed, the dedispersed series depends on DM only through the response,
