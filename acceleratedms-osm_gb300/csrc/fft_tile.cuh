@@ -22,21 +22,21 @@
 
 namespace msosm {
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 // a * (SIGN * i)
 template <int SIGN>
-__device__ __forceinline__ float2 cmul_si(float2 a)
+__host__ __device__ __forceinline__ float2 cmul_si(float2 a)
 {
     return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
 template <int SIGN>
-__device__ __forceinline__ void dft2(float2 *v)
+__host__ __device__ __forceinline__ void dft2(float2 *v)
 {
     float2 t = csub(v[0], v[1]);
     v[0] = cadd(v[0], v[1]);
@@ -44,7 +44,7 @@ __device__ __forceinline__ void dft2(float2 *v)
 }
 
 template <int SIGN>
-__device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3)
+__host__ __device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3)
 {
     float2 a = cadd(v0, v2), b = csub(v0, v2);
     float2 c = cadd(v1, v3), d = cmul_si<SIGN>(csub(v1, v3));
@@ -55,13 +55,13 @@ __device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 
 }
 
 template <int SIGN>
-__device__ __forceinline__ void dft4(float2 *v)
+__host__ __device__ __forceinline__ void dft4(float2 *v)
 {
     dft4<SIGN>(v[0], v[1], v[2], v[3]);
 }
 
 template <int SIGN>
-__device__ __forceinline__ void dft8(float2 *v)
+__host__ __device__ __forceinline__ void dft8(float2 *v)
 {
     const float c = 0.70710678118654752440f;
     float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
@@ -83,22 +83,159 @@ __device__ __forceinline__ void dft8(float2 *v)
     v[7] = csub(e3, t3);
 }
 
+// ---- compile-time twiddles --------------------------------------------------
+// cos/sin of 2*pi*e/R evaluated at compile time by Taylor series after reducing
+// the angle to [-pi/4, pi/4] with the octant symmetries (|x| <= pi/4: 14 terms
+// reach double precision), then rounded to float once.
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+__host__ __device__ constexpr double taylor_sin(double x)
+{
+    double term = x, sum = x;
+    for (int n = 1; n < 14; n++)
+    {
+        term *= -x * x / (double)((2 * n) * (2 * n + 1));
+        sum += term;
+    }
+    return sum;
+}
+__host__ __device__ constexpr double taylor_cos(double x)
+{
+    double term = 1.0, sum = 1.0;
+    for (int n = 1; n < 14; n++)
+    {
+        term *= -x * x / (double)((2 * n - 1) * (2 * n));
+        sum += term;
+    }
+    return sum;
+}
+// angle 2*pi*e/R with e reduced mod R; octant o = floor(8e/R), remainder angle
+__host__ __device__ constexpr double unit_cos(int e, int R)
+{
+    e = ((e % R) + R) % R;
+    const int o8 = 8 * e; // angle = 2*pi*e/R = (pi/4) * (8e/R)
+    const int oct = o8 / R;
+    const double rem = (kTwoPi / 8.0) * ((double)(o8 - oct * R) / (double)R); // in [0, pi/4)
+    // angle = oct*pi/4 + rem
+    switch (oct)
+    {
+    case 0: return taylor_cos(rem);
+    case 1: return taylor_sin(kTwoPi / 8.0 - rem);
+    case 2: return -taylor_sin(rem);
+    case 3: return -taylor_cos(kTwoPi / 8.0 - rem);
+    case 4: return -taylor_cos(rem);
+    case 5: return -taylor_sin(kTwoPi / 8.0 - rem);
+    case 6: return taylor_sin(rem);
+    default: return taylor_cos(kTwoPi / 8.0 - rem);
+    }
+}
+__host__ __device__ constexpr double unit_sin(int e, int R) { return unit_cos(4 * e - R, 4 * R); } // sin t = cos(t - pi/2)
+
+// x * W_R^E with W_R = exp(SIGN * 2*pi*i/R), E known at compile time.
+template <int SIGN, int R, int E>
+__host__ __device__ __forceinline__ float2 cmul_tw(float2 x)
+{
+    constexpr int e = ((E % R) + R) % R;
+    if constexpr (e == 0)
+        return x;
+    else if constexpr (4 * e == R)
+        return cmul_si<SIGN>(x);
+    else if constexpr (2 * e == R)
+        return make_float2(-x.x, -x.y);
+    else if constexpr (4 * e == 3 * R)
+        return cmul_si<-SIGN>(x);
+    else
+    {
+        constexpr float c = (float)unit_cos(e, R);
+        constexpr float s = (float)(SIGN * unit_sin(e, R));
+        return make_float2(x.x * c - x.y * s, x.x * s + x.y * c);
+    }
+}
+
 template <int R, int SIGN>
-__device__ __forceinline__ void dftR(float2 *v)
+__host__ __device__ __forceinline__ void dftR(float2 *v);
+
+// Composite R = A*B in registers (decimation in time, natural-order output):
+//   u_b[ka] = DFT_A{ v[B*a + b] }_a * W_R^(b*ka),   X[ka + A*kb] = DFT_B{ u_b[ka] }_b
+template <int R, int SIGN, int A, int b, int ka>
+__host__ __device__ __forceinline__ void dft_twiddle_row(float2 *t)
+{
+    if constexpr (ka < A)
+    {
+        constexpr int B = R / A;
+        (void)B;
+        t[b * A + ka] = cmul_tw<SIGN, R, b * ka>(t[b * A + ka]);
+        dft_twiddle_row<R, SIGN, A, b, ka + 1>(t);
+    }
+}
+template <int R, int SIGN, int A, int b>
+__host__ __device__ __forceinline__ void dft_first(const float2 *v, float2 *t)
+{
+    constexpr int B = R / A;
+    if constexpr (b < B)
+    {
+        float2 u[A];
+#pragma unroll
+        for (int a = 0; a < A; a++)
+            u[a] = v[B * a + b];
+        dftR<A, SIGN>(u);
+#pragma unroll
+        for (int k = 0; k < A; k++)
+            t[b * A + k] = u[k];
+        dft_twiddle_row<R, SIGN, A, b, 0>(t);
+        dft_first<R, SIGN, A, b + 1>(v, t);
+    }
+}
+template <int R, int SIGN, int A>
+__host__ __device__ __forceinline__ void dft_composite(float2 *v)
+{
+    constexpr int B = R / A;
+    float2 t[R];
+    dft_first<R, SIGN, A, 0>(v, t);
+#pragma unroll
+    for (int ka = 0; ka < A; ka++)
+    {
+        float2 w[B];
+#pragma unroll
+        for (int b = 0; b < B; b++)
+            w[b] = t[b * A + ka];
+        dftR<B, SIGN>(w);
+#pragma unroll
+        for (int kb = 0; kb < B; kb++)
+            v[ka + A * kb] = w[kb];
+    }
+}
+
+template <int R, int SIGN>
+__host__ __device__ __forceinline__ void dftR(float2 *v)
 {
     if constexpr (R == 8)
         dft8<SIGN>(v);
     else if constexpr (R == 4)
         dft4<SIGN>(v);
-    else
+    else if constexpr (R == 2)
         dft2<SIGN>(v);
+    else if constexpr (R == 16)
+        dft_composite<16, SIGN, 8>(v); // 8 x 2
+    else if constexpr (R == 32)
+        dft_composite<32, SIGN, 8>(v); // 8 x 4
+    else
+        dft_composite<R, SIGN, 8>(v); // 8 x R/8
 }
 
-// Radix of the stage that starts with sub-transform size Ns.
-template <int N, int Ns>
+// Radix of the stage that starts with sub-transform size Ns.  The default plan is
+// radix 8 (then 4 or 2); the BIG plan takes two stages of radix 16/32 where it can
+// (threads then hold 32 values, for 256-thread tiles of 8192 points).
+template <int N, int Ns, bool BIG = false>
 struct StageRadix
 {
-    static constexpr int value = (N / Ns >= 8) ? 8 : (N / Ns);
+    static constexpr int rem = N / Ns;
+    static constexpr int big = (N == 512)    ? (Ns == 1 ? 16 : 32)
+                               : (N == 1024) ? 32
+                               : (N == 2048) ? (Ns == 1 ? 16 : (Ns == 16 ? 8 : 16))
+                               : (N == 256)  ? 16
+                               : (N == 128)  ? (Ns == 1 ? 8 : 16)
+                                             : (rem >= 8 ? 8 : rem);
+    static constexpr int value = BIG ? (big < rem ? big : rem) : ((rem >= 8) ? 8 : rem);
 };
 
 template <int N, int COLS>
@@ -133,10 +270,10 @@ struct SmemIO
 // One Stockham stage.  SRC/DST provide load(col, n) / store(col, n, v).
 // SRC_SMEM / DST_SMEM say whether they alias the CTA's shared tile, which decides
 // the barriers.  tw: W_N^m table (SIGN applied), N entries, shared memory.
-template <int N, int COLS, int THREADS, int SIGN, int Ns, bool SRC_SMEM, bool DST_SMEM, class SRC, class DST>
+template <int N, int COLS, int THREADS, int SIGN, int Ns, bool SRC_SMEM, bool DST_SMEM, bool BIG, class SRC, class DST>
 __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const float2 *__restrict__ tw)
 {
-    constexpr int R = StageRadix<N, Ns>::value;
+    constexpr int R = StageRadix<N, Ns, BIG>::value;
     constexpr int NB = COLS * N / R;
     static_assert(NB % THREADS == 0, "butterflies must divide evenly over threads");
     constexpr int BPT = NB / THREADS;
@@ -189,22 +326,23 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
 // Run all stages from Ns onwards.  FIRST: the stage at Ns reads from `first`
 // (global loader) instead of shared memory.  The final stage hands its outputs to
 // `last` (epilogue) instead of shared memory.
-template <int N, int COLS, int THREADS, int SIGN, int Ns, bool FIRST_FROM_LOADER, class LOADER, class EPI>
+template <int N, int COLS, int THREADS, int SIGN, int Ns, bool FIRST_FROM_LOADER, bool BIG = false, class LOADER,
+          class EPI>
 __device__ __forceinline__ void fft_stages(float2 *sm, const float2 *tw, const LOADER &first, const EPI &last)
 {
-    constexpr int R = StageRadix<N, Ns>::value;
+    constexpr int R = StageRadix<N, Ns, BIG>::value;
     constexpr bool IS_LAST = (Ns * R == N);
     SmemIO<N, COLS> io{sm};
     if constexpr (FIRST_FROM_LOADER && IS_LAST)
-        fft_stage<N, COLS, THREADS, SIGN, Ns, false, false>(first, last, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, false, false, BIG>(first, last, tw);
     else if constexpr (FIRST_FROM_LOADER)
-        fft_stage<N, COLS, THREADS, SIGN, Ns, false, true>(first, io, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, false, true, BIG>(first, io, tw);
     else if constexpr (IS_LAST)
-        fft_stage<N, COLS, THREADS, SIGN, Ns, true, false>(io, last, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, true, false, BIG>(io, last, tw);
     else
-        fft_stage<N, COLS, THREADS, SIGN, Ns, true, true>(io, io, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, true, true, BIG>(io, io, tw);
     if constexpr (!IS_LAST)
-        fft_stages<N, COLS, THREADS, SIGN, Ns * R, false>(sm, tw, first, last);
+        fft_stages<N, COLS, THREADS, SIGN, Ns * R, false, BIG>(sm, tw, first, last);
 }
 
 // Twiddle table W_N^m (m < N) into shared memory from a global table of W_N.

@@ -24,7 +24,7 @@ namespace msosm {
 namespace {
 
 constexpr int P_POINTS = 8192;
-constexpr int P_THREADS = 512;
+constexpr int P_THREADS = 256; // 32 points per thread: radix-16/32 stages in registers
 
 template <int N>
 struct PCfg
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             const int c0 = w * C1::COLS;
             PInvLoader ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs, a.rbi + b};
             PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N1, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
-            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true>(sm, tw1, ld, st);
+            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st);
             __threadfence();
             __syncthreads();
             if (threadIdx.x == 0)
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                                          N1,
                                          N2,
                                          1.0f / (float)F};
-            fft_stages<N1, C2::COLS, P_THREADS, +1, 1, false>(sm, tw2, PNoLoad{}, ep);
+            fft_stages<N1, C2::COLS, P_THREADS, +1, 1, false, true>(sm, tw2, PNoLoad{}, ep);
             if constexpr ((MODE & OUT_FOLD) != 0)
             {
                 __syncthreads();
