@@ -314,11 +314,19 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         {
             const int r0 = (w - n1t) * C2::COLS;
             const float2 *src = Ts + (size_t)r0 * N1;
-#pragma unroll 4
-            for (int e = threadIdx.x; e < P_POINTS; e += P_THREADS)
             {
-                const int col = e / N1, n = e % N1;
-                sm[n * C2::LD + col] = __ldcg(src + e);
+                // all of a thread's loads in flight before the first shared store
+                constexpr int PER = P_POINTS / P_THREADS;
+                float2 v[PER];
+#pragma unroll
+                for (int i = 0; i < PER; i++)
+                    v[i] = __ldcg(src + threadIdx.x + i * P_THREADS);
+#pragma unroll
+                for (int i = 0; i < PER; i++)
+                {
+                    const int e = threadIdx.x + i * P_THREADS;
+                    sm[(e % N1) * C2::LD + e / N1] = v[i];
+                }
             }
             if constexpr ((MODE & OUT_FOLD) != 0)
             {
