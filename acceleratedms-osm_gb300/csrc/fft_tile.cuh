@@ -258,6 +258,19 @@ struct HasStoreGroup<T, decltype((void)&T::template store_group<2, 1>, void())>
     static constexpr bool value = true;
 };
 
+// A source may fill a whole stage's inputs at once (load_stage), e.g. to issue all
+// of a thread's independent global loads before using any of them.
+template <class T, class = void>
+struct HasLoadStage
+{
+    static constexpr bool value = false;
+};
+template <class T>
+struct HasLoadStage<T, decltype((void)&T::template load_stage<1, 2, 1, 1, 32>, void())>
+{
+    static constexpr bool value = true;
+};
+
 // Shared-memory source/destination for a stage.
 template <int N, int COLS>
 struct SmemIO
@@ -280,23 +293,31 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
     constexpr int STRIDE = N / R;
     constexpr int TWSTEP = N / (Ns * R);
     float2 v[BPT][R];
-#pragma unroll
-    for (int i = 0; i < BPT; i++)
+    if constexpr (Ns == 1 && HasLoadStage<SRC>::value)
     {
-        const int beta = threadIdx.x + i * THREADS;
-        const int col = beta % COLS;
-        const int j = beta / COLS;
-        const int k = j & (Ns - 1);
+        // butterfly i of this thread: col = beta % COLS, j = beta / COLS, inputs j + r*STRIDE
+        src.template load_stage<BPT, R, STRIDE, COLS, THREADS>(v);
+    }
+    else
+    {
 #pragma unroll
-        for (int r = 0; r < R; r++)
+        for (int i = 0; i < BPT; i++)
         {
-            float2 a = src.load(col, j + r * STRIDE);
-            if constexpr (Ns > 1)
+            const int beta = threadIdx.x + i * THREADS;
+            const int col = beta % COLS;
+            const int j = beta / COLS;
+            const int k = j & (Ns - 1);
+#pragma unroll
+            for (int r = 0; r < R; r++)
             {
-                if (r > 0)
-                    a = cmul(a, tw[r * k * TWSTEP]);
+                float2 a = src.load(col, j + r * STRIDE);
+                if constexpr (Ns > 1)
+                {
+                    if (r > 0)
+                        a = cmul(a, tw[r * k * TWSTEP]);
+                }
+                v[i][r] = a;
             }
-            v[i][r] = a;
         }
     }
     if constexpr (SRC_SMEM && DST_SMEM)

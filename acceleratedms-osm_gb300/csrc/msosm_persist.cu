@@ -96,6 +96,37 @@ struct PInvLoader
         const float2 h = __ldg(Hd + n);
         return cmul(s, h);
     }
+    // The first stage's inputs in two waves: every delay, then every spectrum and
+    // response value, so the delay -> spectrum dependences overlap across elements.
+    template <int BPT, int R, int STRIDE, int COLS, int THREADS>
+    __device__ __forceinline__ void load_stage(float2 (&v)[BPT][R]) const
+    {
+        int slot[BPT][R];
+#pragma unroll
+        for (int i = 0; i < BPT; i++)
+        {
+            const int beta = threadIdx.x + i * THREADS;
+            const int n0 = c0 + beta % COLS + N1 * (beta / COLS);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                slot[i][r] = (int)__ldg(dl + n0 + N1 * STRIDE * r);
+        }
+#pragma unroll
+        for (int i = 0; i < BPT; i++)
+        {
+            const int beta = threadIdx.x + i * THREADS;
+            const int n0 = c0 + beta % COLS + N1 * (beta / COLS);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+            {
+                const int n = n0 + N1 * STRIDE * r;
+                int s = rb - slot[i][r];
+                if (s < 0)
+                    s += fbs;
+                v[i][r] = cmul(__ldcs(ring + (size_t)s * F + n), __ldg(Hd + n));
+            }
+        }
+    }
 };
 
 struct PStoreT
