@@ -1,0 +1,70 @@
+"""The 2-pol int8 batching configuration at reduced length (GPU).
+
+Shape of the configuration: 2-pol psrdada-style int8 I/Q baseband (Gaussian,
+sigma 20, clipped to [-127, 127]), 128 MHz at 820 MHz centre, DMs log-uniform in
+1..1000 (sorted), which forces F = 2^20 (M_min of DM ~1000 is 2^19).  Here: 2^22
+samples per pol and 48 of the trials, so the FP64 oracle can follow; the engine
+runs both pols through the int8 path and folds sqrt(|a|^2+|b|^2) per DM.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def test_two_pol_int8_f2_20(eng, orc):
+    rng = np.random.default_rng(4)
+    dms_all = np.sort(np.exp(rng.uniform(np.log(1.0), np.log(1000.0), 1024))).astype(np.float32)
+    dms = dms_all[::22][:48]
+    dms = np.concatenate([dms, dms_all[-1:]])  # keep the largest DM: it sets M
+    bw, f0 = np.float32(128e6), np.float32(756e6)
+    B = 2
+    N = 1 << 22
+    pols = []
+    for p in range(2):
+        iq = np.clip(np.round(rng.normal(0.0, 20.0, 2 * N)), -127, 127).astype(np.int8)
+        pols.append(iq)
+    ms = [eng.MsosmGpuBatch(bw, dms, f0).initialize(0, B, eng.IN_I8, eng.OUT_C64) for _ in range(2)]
+    assert ms[0].fftpoint == 1 << 20 and ms[0].M == 1 << 19
+    plan = orc.Plan(bw, f0, dms, 0, batch=B)
+    assert plan.M == ms[0].M and plan.delaycount == ms[0].delaycount
+    step = B * ms[0].M
+    K, period = 256, np.float32(0.0071)
+    fold = eng.FoldGpu(period, bw, step, K, len(dms))
+    pick = [0, len(dms) // 2, len(dms) - 1]
+    om = [orc.Msosm(orc.Plan(bw, f0, dms[pick], 1 << 20, batch=B), B, fp64=True) for _ in range(2)]
+    got = [[], []]
+    ref = [[], []]
+    for s in range(N // step):
+        for p in range(2):
+            chunk = np.ascontiguousarray(pols[p][2 * s * step:2 * (s + 1) * step])
+            ms[p].filter_block(chunk)
+            o = np.zeros((len(dms), B, ms[p].M), np.complex64)
+            ms[p].get_output(o)
+            ms[p].synchronize()
+            got[p].append(o[pick])
+            ref[p].append(om[p].process(orc.decode_i8(chunk)))
+        fold.accumulate(ms[0].get_output_pointer(), ms[1].get_output_pointer())
+    w = plan.delaycount + 1  # windows before the ring filled
+    for p in range(2):
+        g = np.concatenate(got[p], axis=1)
+        r = np.concatenate(ref[p], axis=1)
+        for k in range(len(pick)):
+            assert rel_l2(g[k, w:], r[k, w:]) < 1e-4
+    folded, sums, cnts = fold.read()
+    assert cnts.sum() > 0 and np.isfinite(folded).all()
+    # the 2-pol fold of the picked trials equals folding the engine's own series
+    dt = 1.0 / float(bw)
+    for k, d in enumerate(pick):
+        s_ = np.zeros(K)
+        c_ = np.zeros(K, np.uint64)
+        for s in range(N // step):
+            a = got[0][s][k].reshape(-1)
+            b = got[1][s][k].reshape(-1)
+            orc.fold(orc.intensity2(a, b), K, s * step * dt, dt, float(period), s_, c_)
+        assert np.abs(cnts[d].astype(np.int64) - c_.astype(np.int64)).sum() <= 2
+        assert rel_l2(sums[d], s_) < 1e-5
