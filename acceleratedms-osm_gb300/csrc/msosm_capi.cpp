@@ -912,6 +912,90 @@ extern "C" int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long l
     return MSOSM_OK;
 }
 
+// ---- FFT-size autotuning ---------------------------------------------------------
+extern "C" int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch, int in_format,
+                              int min_fftpoint, int max_fftpoint, int steps, int *best_fftpoint, double *best_rate)
+{
+    if (!dms || num_dms <= 0 || batch <= 0 || steps <= 0 || !best_fftpoint || in_elem_bytes(in_format) == 0)
+        return MSOSM_ERR_ARG;
+    // DM subset: up to 16 spread over the list, the largest always included
+    std::vector<float> sub;
+    const int nsub = std::min(num_dms, 16);
+    for (int i = 0; i < nsub; i++)
+        sub.push_back(dms[(long long)i * (num_dms - 1) / std::max(1, nsub - 1)]);
+    sub.back() = dms[num_dms - 1];
+    std::sort(sub.begin(), sub.end());
+    int mmin = 0;
+    for (float d : sub)
+        mmin = std::max(mmin, msosm::plan_min_order(msosm::plan_nd(bw, d, f0)));
+    const long long lo = std::max<long long>(std::max(min_fftpoint, 1 << kMinLog2F), 2ll * mmin);
+    const long long hi = std::min<long long>(max_fftpoint, 1ll << kMaxLog2F);
+    int best = 0;
+    double best_r = 0.0;
+    for (long long F = 1; F <= hi; F <<= 1)
+    {
+        if (F < lo)
+            continue;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        // ring (>= delaycount + batch slots), responses, delays, intermediate, input
+        const int dc = msosm::plan_delaycount(msosm::plan_nd(bw, sub.back(), f0), (int)(F / 2));
+        const double need = (double)F * 8 * (dc + 2 * batch + 64) + (double)sub.size() * F * 10 +
+                            (double)batch * F / 2 * in_elem_bytes(in_format) * 2;
+        if (need > 0.8 * (double)free_b)
+            continue;
+        msosm_t *h = nullptr;
+        if (msosm_create(bw, f0, sub.data(), (int)sub.size(), &h) != MSOSM_OK)
+            continue;
+        int rc = msosm_init(h, (int)F, batch, in_format, MSOSM_OUT_NONE);
+        msosm_fold_t *f = nullptr;
+        if (rc == MSOSM_OK)
+            rc = msosm_fold_create(1.0f, bw, (unsigned long)batch * (F / 2), 64, (int)sub.size(), &f);
+        if (rc == MSOSM_OK)
+            rc = msosm_attach_fold(h, f);
+        void *in = nullptr;
+        const size_t in_bytes = (size_t)batch * (F / 2) * in_elem_bytes(in_format);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (rc == MSOSM_OK && cudaMalloc(&in, in_bytes) == cudaSuccess && cudaMemset(in, 0, in_bytes) == cudaSuccess &&
+            cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess)
+        {
+            rc = msosm_process(h, in, nullptr); // warm-up
+            cudaEventRecord(e0, nullptr);
+            for (int s = 0; rc == MSOSM_OK && s < steps; s++)
+                rc = msosm_process(h, in, nullptr);
+            cudaEventRecord(e1, nullptr);
+            if (rc == MSOSM_OK)
+                rc = msosm_sync(h, nullptr);
+            float ms = 0.f;
+            if (rc == MSOSM_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0.f)
+            {
+                const double rate = (double)steps * batch * (F / 2) * sub.size() / (ms * 1e-3);
+                if (rate > best_r)
+                {
+                    best_r = rate;
+                    best = (int)F;
+                }
+            }
+        }
+        cudaGetLastError();
+        if (e0)
+            cudaEventDestroy(e0);
+        if (e1)
+            cudaEventDestroy(e1);
+        if (in)
+            cudaFree(in);
+        msosm_destroy(h);
+        if (f)
+            msosm_fold_destroy(f);
+    }
+    if (!best)
+        return MSOSM_ERR_UNSUPPORTED;
+    *best_fftpoint = best;
+    if (best_rate)
+        *best_rate = best_r;
+    return MSOSM_OK;
+}
+
 // ---- DM derivative ------------------------------------------------------------------
 extern "C" int msosm_plan_response_derivative(float bw, float f0, float dm, int M, float *H_out)
 {

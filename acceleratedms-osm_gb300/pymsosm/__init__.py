@@ -453,3 +453,42 @@ def read_dat(path) -> np.ndarray:
     re = np.where(re != 0, re - 32768, 0)
     im = np.where(im != 0, im - 32768, 0)
     return (re + 1j * im).astype(np.complex64)
+
+
+def autotune(bw, f0, dms, batch, in_format=IN_C64, min_fftpoint=1 << 16, max_fftpoint=1 << 20, steps=3,
+             cache: str | Path | None = None) -> tuple[int, float]:
+    """Fastest fftpoint for this DM list on this GPU (msosm_autotune), remembered in
+    an optional JSON cache keyed by GPU, band, DM list, batch and input format."""
+    import hashlib
+    import json
+
+    d = np.ascontiguousarray(np.sort(np.atleast_1d(np.asarray(dms, np.float32))))
+    key = None
+    if cache is not None:
+        try:
+            import torch
+
+            gpu = torch.cuda.get_device_name(0)
+        except Exception:
+            gpu = "unknown"
+        key = "|".join([gpu, f"{float(np.float32(bw))}", f"{float(np.float32(f0))}",
+                        hashlib.sha1(d.tobytes()).hexdigest()[:16], str(batch), str(in_format),
+                        str(min_fftpoint), str(max_fftpoint)])
+        p = Path(cache)
+        table = json.loads(p.read_text()) if p.exists() else {}
+        if key in table:
+            return int(table[key]["fftpoint"]), float(table[key]["rate"])
+    best = C.c_int()
+    rate = C.c_double()
+    L = lib()
+    L.msosm_autotune.argtypes = [F, F, P, I, I, I, I, I, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    rc = L.msosm_autotune(bw, f0, d.ctypes.data, len(d), batch, in_format, min_fftpoint, max_fftpoint, steps,
+                          C.byref(best), C.byref(rate))
+    if rc != OK:
+        raise MsosmError(f"autotune: {L.msosm_status_string(rc).decode()}")
+    if cache is not None:
+        p = Path(cache)
+        table = json.loads(p.read_text()) if p.exists() else {}
+        table[key] = {"fftpoint": best.value, "rate": rate.value}
+        p.write_text(json.dumps(table, indent=1))
+    return best.value, rate.value

@@ -142,6 +142,16 @@ int msosm_profile_reset(msosm_t *h);
 int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launches, long long *timed,
                        long long *transforms);
 
+/* ---- FFT-size autotuning ---------------------------------------------------------
+ * No counterpart in the reference (it takes fftpoint from the command line or uses
+ * 2*M_min).  Times fold-only processing of `steps` calls on this GPU for every
+ * power-of-two fftpoint from max(min_fftpoint, 2*M_min) to max_fftpoint whose
+ * buffers fit in free device memory, using at most 16 of the DMs (spread over the
+ * list, the largest always included since it sets the ring), and returns the
+ * fastest in samples x DM trials per second.  The caller caches the answer. */
+int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch, int in_format, int min_fftpoint,
+                   int max_fftpoint, int steps, int *best_fftpoint, double *best_rate);
+
 /* ---- per-DM output files -------------------------------------------------------
  * Replaces MSOSM_DataSave_Uring (data_save/include/msosm_data_save_uring.h:22-52,
  * msosm_data_save_uring.cpp:40-288) with pwrite worker threads (no liburing):

@@ -68,3 +68,14 @@ def test_two_pol_int8_f2_20(eng, orc):
             orc.fold(orc.intensity2(a, b), K, s * step * dt, dt, float(period), s_, c_)
         assert np.abs(cnts[d].astype(np.int64) - c_.astype(np.int64)).sum() <= 2
         assert rel_l2(sums[d], s_) < 1e-5
+
+
+def test_autotune_picks_a_valid_size_and_caches(eng, tmp_path):
+    bw, f0 = np.float32(64e6), np.float32(1368e6)
+    dms = np.linspace(0.0, 200.0, 64).astype(np.float32)
+    cache = tmp_path / "tune.json"
+    F, rate = eng.autotune(bw, f0, dms, 8, eng.IN_C64, 1 << 16, 1 << 20, 2, cache=cache)
+    mmin = eng.plan_min_order(eng.plan_nd(bw, f0, dms))
+    assert F >= 2 * mmin and F <= 1 << 20 and (F & (F - 1)) == 0
+    assert rate > 0
+    assert eng.autotune(bw, f0, dms, 8, eng.IN_C64, 1 << 16, 1 << 20, 2, cache=cache) == (F, rate)
