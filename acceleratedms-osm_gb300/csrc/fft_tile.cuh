@@ -8,8 +8,9 @@
 // instead of shared memory, so a pass touches shared memory only between stages.
 //
 // Shared layout: element (col, n) lives at n*LD + col with LD = COLS + 1.  A
-// warp always covers 16 consecutive columns of one or two rows, so with the pad
-// every access is the minimal two wavefronts for 256 bytes.
+// half-warp covers 16 consecutive columns of one row (column-fast mapping) or 16
+// consecutive rows of one column (j-fast mapping, LD odd), so with the pad every
+// access is the minimal two wavefronts for 256 bytes.
 //
 // Stage (R, Ns):  butterfly j (0 <= j < N/R), k = j mod Ns
 //   in  : x[j + r*N/R] * W_{Ns*R}^{r*k}          (r = 0..R-1)
@@ -271,6 +272,34 @@ struct HasLoadStage<T, decltype((void)&T::template load_stage<1, 2, 1, 1, 32>, v
     static constexpr bool value = true;
 };
 
+// A final-stage destination may ask for the "j-fast" thread mapping (J_FAST):
+// consecutive lanes take consecutive butterflies of one column instead of one
+// butterfly of consecutive columns, so a column's outputs leave as contiguous runs.
+// Its stage twiddles then come from a [r][k] table (tw_last[r*Ns + k] = W_N^(r*k)),
+// which consecutive k read without bank conflicts.
+template <class T, class = void>
+struct IsJFast
+{
+    static constexpr bool value = false;
+};
+template <class T>
+struct IsJFast<T, decltype((void)T::J_FAST, void())>
+{
+    static constexpr bool value = T::J_FAST;
+};
+
+// Ns of the last stage of a plan (the stage with Ns * R == N).
+template <int N, int Ns, bool BIG, bool DONE = (Ns * StageRadix<N, Ns, BIG>::value == N)>
+struct LastNs
+{
+    static constexpr int value = LastNs<N, Ns * StageRadix<N, Ns, BIG>::value, BIG>::value;
+};
+template <int N, int Ns, bool BIG>
+struct LastNs<N, Ns, BIG, true>
+{
+    static constexpr int value = Ns;
+};
+
 // Shared-memory source/destination for a stage.
 template <int N, int COLS>
 struct SmemIO
@@ -282,9 +311,11 @@ struct SmemIO
 
 // One Stockham stage.  SRC/DST provide load(col, n) / store(col, n, v).
 // SRC_SMEM / DST_SMEM say whether they alias the CTA's shared tile, which decides
-// the barriers.  tw: W_N^m table (SIGN applied), N entries, shared memory.
+// the barriers.  tw: W_N^m table (SIGN applied), N entries, shared memory;
+// tw_last: the [r][k] table of a j-fast final stage.
 template <int N, int COLS, int THREADS, int SIGN, int Ns, bool SRC_SMEM, bool DST_SMEM, bool BIG, class SRC, class DST>
-__device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const float2 *__restrict__ tw)
+__device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const float2 *__restrict__ tw,
+                                          const float2 *__restrict__ tw_last = nullptr)
 {
     constexpr int R = StageRadix<N, Ns, BIG>::value;
     constexpr int NB = COLS * N / R;
@@ -292,6 +323,8 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
     constexpr int BPT = NB / THREADS;
     constexpr int STRIDE = N / R;
     constexpr int TWSTEP = N / (Ns * R);
+    constexpr bool JF = IsJFast<DST>::value;
+    static_assert(!JF || Ns * R == N, "the j-fast mapping is for a final stage");
     float2 v[BPT][R];
     if constexpr (Ns == 1 && HasLoadStage<SRC>::value)
     {
@@ -304,8 +337,8 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
         for (int i = 0; i < BPT; i++)
         {
             const int beta = threadIdx.x + i * THREADS;
-            const int col = beta % COLS;
-            const int j = beta / COLS;
+            const int col = JF ? beta / STRIDE : beta % COLS;
+            const int j = JF ? beta % STRIDE : beta / COLS;
             const int k = j & (Ns - 1);
 #pragma unroll
             for (int r = 0; r < R; r++)
@@ -314,7 +347,7 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
                 if constexpr (Ns > 1)
                 {
                     if (r > 0)
-                        a = cmul(a, tw[r * k * TWSTEP]);
+                        a = cmul(a, JF ? tw_last[r * Ns + k] : tw[r * k * TWSTEP]);
                 }
                 v[i][r] = a;
             }
@@ -327,8 +360,8 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
     {
         dftR<R, SIGN>(v[i]);
         const int beta = threadIdx.x + i * THREADS;
-        const int col = beta % COLS;
-        const int j = beta / COLS;
+        const int col = JF ? beta / STRIDE : beta % COLS;
+        const int j = JF ? beta % STRIDE : beta / COLS;
         const int k = j & (Ns - 1);
         const int base = (j / Ns) * Ns * R + k;
         if constexpr (HasStoreGroup<DST>::value)
@@ -347,23 +380,26 @@ __device__ __forceinline__ void fft_stage(const SRC &src, const DST &dst, const 
 // Run all stages from Ns onwards.  FIRST: the stage at Ns reads from `first`
 // (global loader) instead of shared memory.  The final stage hands its outputs to
 // `last` (epilogue) instead of shared memory.
-template <int N, int COLS, int THREADS, int SIGN, int Ns, bool FIRST_FROM_LOADER, bool BIG = false, class LOADER,
-          class EPI>
-__device__ __forceinline__ void fft_stages(float2 *sm, const float2 *tw, const LOADER &first, const EPI &last)
+// EPI_IN_SMEM: the epilogue writes into the shared tile too, so the final stage
+// takes a barrier between its loads and its outputs and another after them.
+template <int N, int COLS, int THREADS, int SIGN, int Ns, bool FIRST_FROM_LOADER, bool BIG = false,
+          bool EPI_IN_SMEM = false, class LOADER, class EPI>
+__device__ __forceinline__ void fft_stages(float2 *sm, const float2 *tw, const LOADER &first, const EPI &last,
+                                           const float2 *tw_last = nullptr)
 {
     constexpr int R = StageRadix<N, Ns, BIG>::value;
     constexpr bool IS_LAST = (Ns * R == N);
     SmemIO<N, COLS> io{sm};
     if constexpr (FIRST_FROM_LOADER && IS_LAST)
-        fft_stage<N, COLS, THREADS, SIGN, Ns, false, false, BIG>(first, last, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, false, EPI_IN_SMEM, BIG>(first, last, tw, tw_last);
     else if constexpr (FIRST_FROM_LOADER)
         fft_stage<N, COLS, THREADS, SIGN, Ns, false, true, BIG>(first, io, tw);
     else if constexpr (IS_LAST)
-        fft_stage<N, COLS, THREADS, SIGN, Ns, true, false, BIG>(io, last, tw);
+        fft_stage<N, COLS, THREADS, SIGN, Ns, true, EPI_IN_SMEM, BIG>(io, last, tw, tw_last);
     else
         fft_stage<N, COLS, THREADS, SIGN, Ns, true, true, BIG>(io, io, tw);
     if constexpr (!IS_LAST)
-        fft_stages<N, COLS, THREADS, SIGN, Ns * R, false, BIG>(sm, tw, first, last);
+        fft_stages<N, COLS, THREADS, SIGN, Ns * R, false, BIG, EPI_IN_SMEM>(sm, tw, first, last, tw_last);
 }
 
 // Twiddle table W_N^m (m < N) into shared memory from a global table of W_N.

@@ -50,17 +50,15 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
 
 // Called by one thread: wait until *cnt >= target.  False if the launch failed
 // meanwhile (another CTA raised the error flag) or this wait timed out (raises it).
-// Polls with volatile loads (served by L2, no L1 invalidation), then one
-// acquire load orders the caller's later reads after the observed count.
+// One acquire load when the count is already there (the common case); otherwise
+// polls with volatile loads (served by L2, no L1 invalidation), then one acquire
+// load orders the caller's later reads after the observed count.
 __device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target, int *err,
                                            unsigned long long timeout_ns)
 {
-    const volatile unsigned *vc = cnt;
-    if (*vc >= target)
-    {
-        (void)ld_acquire(cnt);
+    if (ld_acquire(cnt) >= target)
         return true;
-    }
+    const volatile unsigned *vc = cnt;
     const uint64_t t0 = global_ns();
     unsigned backoff = 32;
     while (*vc < target)
@@ -78,6 +76,20 @@ __device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target,
     }
     (void)ld_acquire(cnt);
     return true;
+}
+
+// Streaming read-only loads that skip L1 allocation, leaving L1 to the twiddle tables.
+__device__ __forceinline__ float2 ld_na(const float2 *p)
+{
+    float2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int ld_na(const uint16_t *p)
+{
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return (int)v;
 }
 
 struct PInvLoader
@@ -109,7 +121,7 @@ struct PInvLoader
             const int n0 = c0 + beta % COLS + N1 * (beta / COLS);
 #pragma unroll
             for (int r = 0; r < R; r++)
-                slot[i][r] = (int)__ldg(dl + n0 + N1 * STRIDE * r);
+                slot[i][r] = ld_na(dl + n0 + N1 * STRIDE * r);
         }
 #pragma unroll
         for (int i = 0; i < BPT; i++)
@@ -123,24 +135,28 @@ struct PInvLoader
                 int s = rb - slot[i][r];
                 if (s < 0)
                     s += fbs;
-                v[i][r] = cmul(__ldcs(ring + (size_t)s * F + n), __ldg(Hd + n));
+                v[i][r] = cmul(ld_na(ring + (size_t)s * F + n), ld_na(Hd + n));
             }
         }
     }
 };
 
+// Pass-1 outputs into the slot, column-major: element (n1, k2) at n1*N2 + k2, so
+// that pass 2 reads a row tile's inputs as 128-byte runs straight into registers.
+// The last stage runs j-fast, so a column's outputs leave as contiguous runs too.
 struct PStoreT
 {
+    static constexpr bool J_FAST = true;
     float2 *T;
     const float2 *lo, *hi;
-    int c0, N1;
+    int c0, N2;
     unsigned n2_mask;
     int n2_shift;
     __device__ __forceinline__ void store(int col, int k2, float2 v) const
     {
         const int n1 = c0 + col;
         const float2 w = twiddle_F(lo, hi, (unsigned)(n1 * k2), n2_mask, n2_shift);
-        T[n1 + (size_t)N1 * k2] = cmul(v, w);
+        T[(size_t)n1 * N2 + k2] = cmul(v, w);
     }
     // Last stage: outputs k2 = base + r*Ns.  W_F^(n1*k2) = W_F^(n1*base) * (W_F^(n1*Ns))^r,
     // two table lookups per butterfly and a product chain instead of two per output.
@@ -150,12 +166,37 @@ struct PStoreT
         const int n1 = c0 + col;
         float2 w = twiddle_F(lo, hi, (unsigned)(n1 * base), n2_mask, n2_shift);
         const float2 step = twiddle_F(lo, hi, (unsigned)(n1 * Ns), n2_mask, n2_shift);
-        float2 *dst = T + n1 + (size_t)N1 * base;
+        float2 *dst = T + (size_t)n1 * N2 + base;
 #pragma unroll
         for (int r = 0; r < R; r++)
         {
-            dst[(size_t)N1 * Ns * r] = cmul(v[r], w);
+            dst[Ns * r] = cmul(v[r], w);
             w = cmul(w, step);
+        }
+    }
+};
+
+// Pass-2 inputs of row tile r0 .. r0+COLS-1 from the column-major slot: element
+// (row r0 + col, n1) at n1*N2 + r0 + col.  L2-resident, so loaded with .cg.
+struct PTLoader
+{
+    const float2 *Ts;
+    int r0, N2;
+    __device__ __forceinline__ float2 load(int col, int n1) const
+    {
+        return __ldcg(Ts + (size_t)n1 * N2 + r0 + col);
+    }
+    template <int BPT, int R, int STRIDE, int COLS, int THREADS>
+    __device__ __forceinline__ void load_stage(float2 (&v)[BPT][R]) const
+    {
+#pragma unroll
+        for (int i = 0; i < BPT; i++)
+        {
+            const int beta = threadIdx.x + i * THREADS;
+            const float2 *p = Ts + r0 + beta % COLS + (size_t)N2 * (beta / COLS);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                v[i][r] = __ldcg(p + (size_t)N2 * STRIDE * r);
         }
     }
 };
@@ -203,8 +244,16 @@ struct PEpilogue
 // period, and phase is monotone within a run) is summed in registers and lands as
 // one shared atomic; other runs go sample by sample.  Zero samples are skipped as
 // foldDataPhase_kernel does.
+// One phase bin of the per-CTA accumulator: the sum and the count side by side, so
+// that the whole shared layout sits at compile-time offsets.
+struct BinAcc
+{
+    float sum;
+    unsigned cnt;
+};
+
 template <int COLS, int HALF>
-__device__ __forceinline__ void fold_tile(const float *s_p, float *s_sum, unsigned *s_cnt, uint64_t ph_b,
+__device__ __forceinline__ void fold_tile(const float *s_p, BinAcc *s_bins, uint64_t ph_b,
                                           uint64_t dphase, unsigned K, int r0, int N2)
 {
     constexpr int SAMPLES = COLS * HALF;
@@ -235,8 +284,8 @@ __device__ __forceinline__ void fold_tile(const float *s_p, float *s_sum, unsign
             }
             if (n)
             {
-                atomicAdd(s_sum + bf, s);
-                atomicAdd(s_cnt + bf, n);
+                atomicAdd(&s_bins[bf].sum, s);
+                atomicAdd(&s_bins[bf].cnt, n);
             }
         }
         else
@@ -247,10 +296,30 @@ __device__ __forceinline__ void fold_tile(const float *s_p, float *s_sum, unsign
                 if (p[i] != 0.0f)
                 {
                     const unsigned bi = phase_bin(ph0 + (uint64_t)i * dphase, K);
-                    atomicAdd(s_sum + bi, p[i]);
-                    atomicAdd(s_cnt + bi, 1u);
+                    atomicAdd(&s_bins[bi].sum, p[i]);
+                    atomicAdd(&s_bins[bi].cnt, 1u);
                 }
             }
+        }
+    }
+}
+
+// Per-CTA fold accumulator: the shared per-bin sums of one DM trial, carried over
+// the CTA's consecutive pass-2 items of that trial and flushed to the global
+// double / u64 sums when the trial changes and at the end.  Each thread flushes and
+// clears the bins it owns; the callers' barriers order this against fold_tile().
+__device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, int d)
+{
+    double *gs = fa.sum + (size_t)d * fa.K;
+    unsigned long long *gc = fa.cnt + (size_t)d * fa.K;
+    for (unsigned i = threadIdx.x; i < fa.K; i += P_THREADS)
+    {
+        const BinAcc v = s_bins[i];
+        if (v.cnt)
+        {
+            atomicAdd(gs + i, (double)v.sum);
+            atomicAdd(gc + i, (unsigned long long)v.cnt);
+            s_bins[i] = BinAcc{0.0f, 0u};
         }
     }
 }
@@ -266,22 +335,42 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     constexpr int per_block = n1t + n2t;
     constexpr int F = N1 * N2;
     constexpr int M = F / 2;
+    constexpr int NSL = LastNs<N2, 1, true>::value;     // pass 1, last stage: Ns
+    constexpr int R2F = StageRadix<N1, 1, true>::value; // pass 2, first stage: radix
+    // two-stage pass 1 (radix R1F then the last stage): its only stage twiddles are
+    // the last stage's, so the [r][k] table replaces the W_{N2} table
+    constexpr bool P1_TWO = NSL == StageRadix<N2, 1, true>::value;
+    constexpr bool FOLD = (MODE & OUT_FOLD) != 0;
+    static_assert(C2::COLS * (N1 / 2) <= 2 * DATA, "fold staging fits in the data tile");
     extern __shared__ float2 smem[];
     float2 *sm = smem;
-    float2 *tw1 = smem + DATA; // W_{N2}: pass-1 stages
-    float2 *tw2 = tw1 + N2;    // W_{N1}: pass-2 stages
-    float *s_p = reinterpret_cast<float *>(tw2 + N1); // fold staging tile (C2::COLS * N1/2 floats)
-    float *s_sum = s_p + (((MODE & OUT_FOLD) != 0) ? C2::COLS * (N1 / 2) : 0);
-    unsigned *s_cnt = reinterpret_cast<unsigned *>(s_sum + (((MODE & OUT_FOLD) != 0) ? a.fold.K : 0));
+    float2 *tw2 = smem + DATA;                // W_{N1}: pass-2 stages
+    float2 *tw1L = tw2 + N1;                  // pass-1 last stage, [r][k] = W_{N2}^(r*k)
+    float2 *tw1 = P1_TWO ? tw1L : tw1L + N2;  // W_{N2}: pass-1 middle stages
+    // fold staging tile (C2::COLS * N1/2 floats) in the data tile: pass 2's last stage
+    // reads all its inputs before the epilogue writes it
+    float *s_p = reinterpret_cast<float *>(sm);
+    BinAcc *s_bins = reinterpret_cast<BinAcc *>(tw1L + (P1_TWO ? N2 : 2 * N2)); // K bins
     // (ticket, verdict) published by thread 0; double-buffered by iteration parity
     // so a skipped item (no barrier inside) cannot overwrite what slow threads read
     __shared__ unsigned s_ticket[2];
     __shared__ int s_verdict[2];
 
     for (int i = threadIdx.x; i < N2; i += P_THREADS)
-        tw1[i] = __ldg(a.tw.twN2 + i);
+    {
+        const int r = i / NSL, k = i % NSL; // r*k < N2
+        tw1L[i] = __ldg(a.tw.twN2 + r * k);
+        if constexpr (!P1_TWO)
+            tw1[i] = __ldg(a.tw.twN2 + i);
+    }
     for (int i = threadIdx.x; i < N1; i += P_THREADS)
         tw2[i] = __ldg(a.tw.twN1 + i);
+    if constexpr (FOLD)
+    {
+        for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
+            s_bins[i] = BinAcc{0.0f, 0u};
+    }
+    int fold_d = -1; // the DM trial s_bins holds (uniform over the CTA)
 
     const long long total = (a.G + a.lag) * (long long)per_block;
     const int B = a.B;
@@ -334,41 +423,33 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         {
             const int c0 = w * C1::COLS;
             PInvLoader ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs, a.rbi + b};
-            PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N1, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
-            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st);
-            __threadfence();
+            PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N2, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
+            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st, tw1L);
+            // publish: the barrier orders every thread's stores before thread 0's
+            // gpu-scope fence (fences are cumulative), which precedes the count
             __syncthreads();
             if (threadIdx.x == 0)
+            {
+                __threadfence();
                 atomicAdd(a.p1_done + slot, 1u);
+            }
         }
         else
         {
             const int r0 = (w - n1t) * C2::COLS;
-            const float2 *src = Ts + (size_t)r0 * N1;
+            if constexpr (FOLD)
             {
-                // all of a thread's loads in flight before the first shared store
-                constexpr int PER = P_POINTS / P_THREADS;
-                float2 v[PER];
-#pragma unroll
-                for (int i = 0; i < PER; i++)
-                    v[i] = __ldcg(src + threadIdx.x + i * P_THREADS);
-#pragma unroll
-                for (int i = 0; i < PER; i++)
+                if (d != fold_d)
                 {
-                    const int e = threadIdx.x + i * P_THREADS;
-                    sm[(e % N1) * C2::LD + e / N1] = v[i];
+                    if (fold_d >= 0)
+                        fold_flush(s_bins, a.fold, fold_d);
+                    fold_d = d;
                 }
             }
-            if constexpr ((MODE & OUT_FOLD) != 0)
-            {
-                for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
-                {
-                    s_sum[i] = 0.0f;
-                    s_cnt[i] = 0u;
-                }
-            }
-            __syncthreads();
-            // the slot may be refilled as soon as every thread holds its data
+            // first stage straight from the slot; its closing barrier means every
+            // thread holds its inputs, so the slot may be refilled
+            SmemIO<N1, C2::COLS> io{sm};
+            fft_stage<N1, C2::COLS, P_THREADS, +1, 1, false, true, true>(PTLoader{Ts, r0, N2}, io, tw2);
             if (threadIdx.x == 0)
                 atomicAdd(a.p2_done + slot, 1u);
             const size_t row = ((size_t)d * B + b) * M;
@@ -379,27 +460,20 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                                          N1,
                                          N2,
                                          1.0f / (float)F};
-            fft_stages<N1, C2::COLS, P_THREADS, +1, 1, false, true>(sm, tw2, PNoLoad{}, ep);
-            if constexpr ((MODE & OUT_FOLD) != 0)
+            fft_stages<N1, C2::COLS, P_THREADS, +1, R2F, false, true, FOLD>(sm, tw2, PNoLoad{}, ep);
+            if constexpr (FOLD)
             {
-                __syncthreads();
-                fold_tile<C2::COLS, N1 / 2>(s_p, s_sum, s_cnt,
+                fold_tile<C2::COLS, N1 / 2>(s_p, s_bins,
                                             a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
                                             a.fold.dphase, a.fold.K, r0, N2);
-                __syncthreads();
-                double *gs = a.fold.sum + (size_t)d * a.fold.K;
-                unsigned long long *gc = a.fold.cnt + (size_t)d * a.fold.K;
-                for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
-                {
-                    const unsigned c = s_cnt[i];
-                    if (c)
-                    {
-                        atomicAdd(gs + i, (double)s_sum[i]);
-                        atomicAdd(gc + i, (unsigned long long)c);
-                    }
-                }
+                // s_p and the bins are next touched after the next ticket barrier
             }
         }
+    }
+    if constexpr (FOLD)
+    {
+        if (fold_d >= 0)
+            fold_flush(s_bins, a.fold, fold_d);
     }
 }
 
@@ -410,8 +484,9 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     using C2 = PCfg<N1>;
     constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
     auto k = inv_persistent_kernel<N1, N2, MODE>;
-    const size_t smem = (size_t)(DATA + N1 + N2) * sizeof(float2) +
-                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 + (size_t)C2::COLS * (N1 / 2) * 4 : 0);
+    constexpr bool P1_TWO = LastNs<N2, 1, true>::value == StageRadix<N2, 1, true>::value;
+    const size_t smem = (size_t)(DATA + N1 + (P1_TWO ? N2 : 2 * N2)) * sizeof(float2) +
+                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
     static size_t granted[kMaxDevices] = {};
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
