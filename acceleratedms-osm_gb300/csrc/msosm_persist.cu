@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                 verdict = 0;
                 if (f >= 0 && f < a.G)
                 {
-                    const int slot = (int)(f % a.S);
-                    const unsigned gen = (unsigned)(f / a.S);
+                    const unsigned slot = (unsigned)f % (unsigned)a.S; // f < 2^31 (host check)
+                    const unsigned gen = (unsigned)f / (unsigned)a.S;
                     const bool ok = p1 ? wait_count(a.p2_done + slot, gen * n2t, a.err, a.timeout_ns)
                                        : wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, a.timeout_ns);
                     verdict = ok ? 1 : 0;
@@ -415,10 +415,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         const int w = (int)(t % per_block);
         const bool is_p1 = w < n1t;
         const long long f = is_p1 ? q : q - a.lag;
-        const int slot = (int)(f % a.S);
+        const int slot = (int)((unsigned)f % (unsigned)a.S);
         float2 *Ts = a.T + (size_t)slot * F;
         const long long gi = a.g0 + f;
-        const int d = (int)(gi / B), b = (int)(gi % B);
+        const int d = (int)((unsigned)gi / (unsigned)B), b = (int)((unsigned)gi % (unsigned)B);
         if (is_p1)
         {
             const int c0 = w * C1::COLS;
@@ -510,7 +510,9 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
         plan->grid = grid;
         return cudaSuccess;
     }
-    if (a.S <= a.lag)
+    // the kernel indexes transforms and tickets in 32 bits
+    if (a.S <= a.lag || a.g0 < 0 || a.G < 0 || a.g0 + a.G + a.lag >= (1ll << 31) ||
+        (a.G + a.lag) * (long long)per_block >= (1ll << 32))
         return cudaErrorInvalidValue;
     k<<<grid, P_THREADS, smem, st>>>(a);
     return cudaGetLastError();
