@@ -254,6 +254,69 @@ def run_reference(args, w, rank, world):
 
 
 # ----------------------------------------------------------------------------
+CUFFT_LIB = ROOT / "baseline" / "cufft_pipeline" / "lib" / "libmsosm_cufft_pipeline.so"
+
+
+def cufft_design_rate(proc, dms, dinp, w, calls, steps, stream, engine_folded):
+    """The reference's GPU design (cuFFT forward, delayed-bin gather x response, batched
+    cuFFT inverse, discard + fold) restated in baseline/cufft_pipeline and timed on the same
+    workload, device-resident input, CUDA events; the engine's plan tables are reused."""
+    import ctypes as C
+
+    import torch
+
+    if not CUFFT_LIB.exists():
+        return {"unavailable": f"{CUFFT_LIB.relative_to(ROOT)} not built"}
+    L = C.CDLL(str(CUFFT_LIB))
+    L.mcp_create.argtypes = [C.c_int] * 6 + [C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
+    L.mcp_process.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.mcp_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.mcp_reset_fold.argtypes = [C.c_void_p, C.c_void_p]
+    L.mcp_destroy.argtypes = [C.c_void_p]
+    dev = dinp.device
+    D, F, M, B = len(dms), proc.fftpoint, proc.M, proc.batch
+    H = torch.empty((D, F), dtype=torch.complex64, device=dev)
+    dl = torch.empty((D, F), dtype=torch.int16, device=dev)
+    for i in range(D):
+        H[i] = torch.from_numpy(proc.response(i))
+        dl[i] = torch.from_numpy(proc.delay_points(i).astype(np.uint16).view(np.int16))
+    chunk = 64
+    h = C.c_void_p()
+    rc = L.mcp_create(int(np.log2(F)), B, D, proc.ring_blocks, chunk, w["nbins"], np.float32(w["period"]),
+                      np.float32(w["bw"]), H.data_ptr(), dl.data_ptr(), C.byref(h))
+    if rc != 0:
+        return {"unavailable": f"mcp_create failed ({rc})"}
+    sp = C.c_void_p(stream.cuda_stream)
+    try:
+        def step():
+            L.mcp_reset_fold(h, sp)
+            for c in range(calls):
+                rc = L.mcp_process(h, C.c_void_p(dinp.data_ptr() + c * B * M * 8), sp)
+                if rc != 0:
+                    raise RuntimeError(f"mcp_process failed ({rc})")
+
+        step()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t_ms = ev0.elapsed_time(ev1)
+        sums = np.zeros((D, w["nbins"]))
+        cnts = np.zeros((D, w["nbins"]), np.uint64)
+        L.mcp_read(h, sums.ctypes.data, cnts.ctypes.data)
+    finally:
+        L.mcp_destroy(h)
+    folded = sums / np.maximum(cnts, 1)
+    diff = float(np.linalg.norm(folded - engine_folded) / np.linalg.norm(engine_folded))
+    return {"value": calls * B * M * D * steps / (t_ms * 1e-3), "unit": UNIT, "ms_per_step": t_ms / steps,
+            "kind": "the reference's cuFFT pipeline restated (baseline/cufft_pipeline): cuFFT forward, "
+                    "gather x response, batched cuFFT inverse in DM chunks of %d, fused discard + fold" % chunk,
+            "folded_rel_l2_vs_engine": diff}
+
+
 def run_engine(args, w, rank, world, local):
     import torch
 
@@ -369,6 +432,9 @@ def run_engine(args, w, rank, world, local):
                    "parallelism": f"dm-shard x{world}"},
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "check": check,
     }
+    if world == 1 and not args.no_cufft_baseline:
+        line["reference_gpu_design"] = cufft_design_rate(proc, dms, dinp, w, calls, args.steps, stream,
+                                                         folded_host)
     if world == 1 and not args.no_cpu_baseline:
         rate, sec, desc, cores, _ = cpu_port_rate(w, 64, 4)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
@@ -383,6 +449,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_dm_512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cufft-baseline", action="store_true",
+                    help="skip timing the cuFFT restatement of the reference's GPU design")
     ap.add_argument("--samples", type=int, default=0, help="override the baseband length (profiling captures)")
     ap.add_argument("--dm-trials", type=int, default=0, help="override the DM-trial count (profiling captures)")
     args = ap.parse_args()
