@@ -913,6 +913,15 @@ extern "C" int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long l
 }
 
 // ---- FFT-size autotuning ---------------------------------------------------------
+extern "C" int msosm_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
+                                   unsigned long long *elapsed_ns)
+{
+    if (!timed_out || !elapsed_ns || timeout_ns == 0 || timeout_ns > kWaitTimeoutNs)
+        return MSOSM_ERR_ARG;
+    const cudaError_t e = msosm::persist_selftest_wait(preset, target, timeout_ns, timed_out, elapsed_ns);
+    return e == cudaSuccess ? MSOSM_OK : MSOSM_ERR_CUDA;
+}
+
 extern "C" int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch, int in_format,
                               int min_fftpoint, int max_fftpoint, int steps, int *best_fftpoint, double *best_rate)
 {

@@ -548,7 +548,51 @@ cudaError_t persist_dispatch(int L, const PersistArgs &a, int sms, cudaStream_t 
     }
 }
 
+// One thread runs wait_count() on a counter: `preset` is written first, the wait asks
+// for `target`.  Nothing else writes the counter, so a preset below the target makes
+// the wait run out; the flag and the elapsed %globaltimer time come back.
+__global__ void selftest_wait_kernel(unsigned *cnt, unsigned preset, unsigned target, int *err,
+                                     unsigned long long timeout_ns, unsigned long long *elapsed_ns)
+{
+    *cnt = preset;
+    __threadfence();
+    const uint64_t t0 = global_ns();
+    (void)wait_count(cnt, target, err, timeout_ns); // a timeout sets *err
+    *elapsed_ns = global_ns() - t0;
+}
+
 } // namespace
+
+cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
+                                  unsigned long long *elapsed_ns)
+{
+    struct Buf
+    {
+        unsigned cnt;
+        int err;
+        unsigned long long elapsed;
+    };
+    Buf *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(Buf));
+    if (e != cudaSuccess)
+        return e;
+    e = cudaMemset(d, 0, sizeof(Buf));
+    if (e == cudaSuccess)
+    {
+        selftest_wait_kernel<<<1, 1>>>(&d->cnt, preset, target, &d->err, timeout_ns, &d->elapsed);
+        e = cudaGetLastError();
+    }
+    Buf h{};
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&h, d, sizeof(Buf), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e == cudaSuccess)
+    {
+        *timed_out = h.err;
+        *elapsed_ns = h.elapsed;
+    }
+    return e;
+}
 
 bool persist_supported(int L) { return L >= 16 && L <= 22; }
 

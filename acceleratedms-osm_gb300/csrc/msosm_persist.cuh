@@ -31,6 +31,9 @@ struct PersistPlan
 };
 
 bool persist_supported(int L);
+// The persistent kernel's bounded wait, run alone (see msosm_selftest_wait).
+cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
+                                  unsigned long long *elapsed_ns);
 // Grid and ring geometry for the given sizes / output mode (no launch).
 cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan);
 cudaError_t launch_inverse_persistent(int L, const PersistArgs &a, int sms, cudaStream_t st);

@@ -492,3 +492,18 @@ def autotune(bw, f0, dms, batch, in_format=IN_C64, min_fftpoint=1 << 16, max_fft
         table[key] = {"fftpoint": best.value, "rate": rate.value}
         p.write_text(json.dumps(table, indent=1))
     return best.value, rate.value
+
+
+def selftest_wait(preset: int, target: int, timeout_ns: int) -> tuple[bool, int]:
+    """Run the persistent transform's bounded device-side wait alone on a counter preset
+    to `preset` (nothing else writes it), waiting for `target` (msosm_selftest_wait).
+    Returns (timed_out, elapsed_ns)."""
+    L = lib()
+    L.msosm_selftest_wait.argtypes = [C.c_uint, C.c_uint, C.c_ulonglong, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_ulonglong)]
+    t = C.c_int()
+    e = C.c_ulonglong()
+    rc = L.msosm_selftest_wait(preset, target, timeout_ns, C.byref(t), C.byref(e))
+    if rc != OK:
+        raise MsosmError(f"selftest_wait: {L.msosm_status_string(rc).decode()}")
+    return bool(t.value), int(e.value)

@@ -152,6 +152,14 @@ int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launch
 int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch, int in_format, int min_fftpoint,
                    int max_fftpoint, int steps, int *best_fftpoint, double *best_rate);
 
+/* Failure-detection self-test (no counterpart in the reference): runs the persistent
+ * transform's bounded device-side wait alone, on a counter preset to `preset` that
+ * nothing else writes, waiting for `target` with a limit of timeout_ns (at most 2 s).
+ * *timed_out = 1 when the wait ran out (the kernel raised its error flag and returned;
+ * the context stays usable), *elapsed_ns = the wait's duration on %globaltimer. */
+int msosm_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
+                        unsigned long long *elapsed_ns);
+
 /* ---- per-DM output files -------------------------------------------------------
  * Replaces MSOSM_DataSave_Uring (data_save/include/msosm_data_save_uring.h:22-52,
  * msosm_data_save_uring.cpp:40-288) with pwrite worker threads (no liburing):
