@@ -195,6 +195,7 @@ struct msosm_fold_s
     double *d_sum = nullptr;
     unsigned long long *d_cnt = nullptr;
     float *d_folded = nullptr;
+    float *d_pair = nullptr; // 2-pol fused fold: the first polarisation's |a|^2, num_series*size
     std::string err;
 
     msosm::FoldArgs args() const
@@ -212,6 +213,7 @@ struct msosm_fold_s
         dfree(d_sum);
         dfree(d_cnt);
         dfree(d_folded);
+        dfree(d_pair);
     }
 };
 
@@ -248,6 +250,8 @@ struct msosm_s
     long long step = 0;
     msosm_fold_t *fold = nullptr;
     msosm_writer_s *writer = nullptr;
+    float *pair_out = nullptr;      // first polarisation of a 2-pol fused fold: |a|^2 goes here
+    const float *pair_in = nullptr; // second polarisation: folds sqrt(pair_in + |b|^2)
     Profiler prof;
     std::string err;
 
@@ -711,7 +715,11 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     {
         a.out_mode |= msosm::OUT_FOLD;
         a.fold = h->fold->args();
+        if (h->pair_in)
+            a.out_mode |= msosm::OUT_PAIR;
     }
+    if (h->pair_out)
+        a.out_mode |= msosm::OUT_POW;
     const long long total = (long long)h->D * h->B;
     if (h->persist)
     {
@@ -729,6 +737,8 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         pa.out_mode = a.out_mode;
         pa.out_c64 = a.out_c64;
         pa.out_u16 = a.out_u16;
+        pa.out_pow = h->pair_out;
+        pa.pair_pow = h->pair_in;
         pa.fold = a.fold;
         pa.ticket = h->d_sync;
         pa.p1_done = h->d_sync + 1;
@@ -810,7 +820,7 @@ extern "C" int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *
         return h->fail(MSOSM_ERR_STATE, "msosm_process before msosm_init");
     if (!in || nsteps < 0)
         return h->fail(MSOSM_ERR_ARG, "null input");
-    if (h->out_mode == MSOSM_OUT_NONE && !h->fold)
+    if (h->out_mode == MSOSM_OUT_NONE && !h->fold && !h->pair_out)
         return h->fail(MSOSM_ERR_STATE, "no output mode and no fold attached");
     cudaStream_t st = (cudaStream_t)stream;
     // device input is read in place only when aligned to its element size (the
@@ -1308,6 +1318,8 @@ extern "C" int msosm_attach_fold(msosm_t *h, msosm_fold_t *f)
 {
     if (!h)
         return MSOSM_ERR_ARG;
+    h->pair_in = nullptr;
+    h->pair_out = nullptr;
     if (!f)
     {
         h->fold = nullptr;
@@ -1329,5 +1341,41 @@ extern "C" int msosm_attach_fold(msosm_t *h, msosm_fold_t *f)
     if ((double)f->P / f->dt <= span)
         return h->fail(MSOSM_ERR_UNSUPPORTED, "fold period shorter than the fused epilogue's sample span");
     h->fold = f;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_attach_fold_pol2(msosm_t *first, msosm_t *second, msosm_fold_t *f)
+{
+    if (!first || !second || first == second)
+        return MSOSM_ERR_ARG;
+    if (!f)
+    {
+        msosm_attach_fold(first, nullptr);
+        return msosm_attach_fold(second, nullptr);
+    }
+    if (!first->inited || !second->inited)
+        return second->fail(MSOSM_ERR_STATE, "attach_fold_pol2 before init");
+    if (first->D != second->D || first->B != second->B || first->M != second->M || first->dms != second->dms)
+        return second->fail(MSOSM_ERR_ARG, "attach_fold_pol2: both polarisations need the same DMs, batch and size");
+    if (!first->persist || !second->persist)
+        return second->fail(MSOSM_ERR_UNSUPPORTED, "the fused 2-pol fold needs fftpoint >= 65536");
+    if (first->out_mode != MSOSM_OUT_NONE || second->out_mode != MSOSM_OUT_NONE)
+        return second->fail(MSOSM_ERR_UNSUPPORTED, "the fused 2-pol fold needs both handles in MSOSM_OUT_NONE");
+    int rc = msosm_attach_fold(second, f); // the fold checks (sizes, bins, period span)
+    if (rc != MSOSM_OK)
+        return rc;
+    const size_t n = (size_t)second->D * second->B * second->M;
+    if (!f->d_pair)
+    {
+        cudaError_t e = dalloc(&f->d_pair, n);
+        if (e != cudaSuccess)
+        {
+            msosm_attach_fold(second, nullptr);
+            return second->cuda_fail(e, "cudaMalloc(2-pol power)");
+        }
+    }
+    msosm_attach_fold(first, nullptr);
+    first->pair_out = f->d_pair;
+    second->pair_in = f->d_pair;
     return MSOSM_OK;
 }

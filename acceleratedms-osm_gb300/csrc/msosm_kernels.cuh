@@ -18,6 +18,8 @@ enum OutMode : int
     OUT_C64 = 1,  // float2 [D][B][M] (fold-mode output buffer of the reference)
     OUT_U16 = 2,  // uint16_pair [D][B][M] (discardSamplesToUint16)
     OUT_FOLD = 4, // |x|^2 phase fold of every DM (fused)
+    OUT_POW = 8,  // float |x|^2 [D][B][M] for the second polarisation's fused fold
+    OUT_PAIR = 16 // with OUT_FOLD: fold sqrt(partner |a|^2 + |x|^2) (2-pol intensity)
 };
 
 // F = N1 * N2, N2 = 2^ceil(L/2), N1 = 2^floor(L/2).

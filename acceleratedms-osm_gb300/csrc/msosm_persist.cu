@@ -215,6 +215,8 @@ struct PEpilogue
 {
     float2 *out_c64;
     uint32_t *out_u16;
+    float *out_pow;
+    const float *pair_pow;
     float *s_p;
     int r0, N1, N2;
     float scale;
@@ -233,7 +235,14 @@ struct PEpilogue
                 out_c64[o] = x;
             if constexpr ((MODE & OUT_U16) != 0)
                 out_u16[o] = encode_u16(x);
-            if constexpr ((MODE & OUT_FOLD) != 0)
+            if constexpr ((MODE & OUT_POW) != 0)
+                out_pow[o] = x.x * x.x + x.y * x.y;
+            if constexpr ((MODE & OUT_PAIR) != 0)
+            {
+                // 2-pol intensity sqrt(|a|^2 + |b|^2) (calculateIntensity, gpu_kernel.cu:430-440)
+                s_p[k1h * COLS + col] = sqrtf(__ldcs(pair_pow + o) + (x.x * x.x + x.y * x.y));
+            }
+            else if constexpr ((MODE & OUT_FOLD) != 0)
                 s_p[k1h * COLS + col] = x.x * x.x + x.y * x.y;
         }
     }
@@ -455,6 +464,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             const size_t row = ((size_t)d * B + b) * M;
             PEpilogue<MODE, C2::COLS> ep{a.out_c64 ? a.out_c64 + row : nullptr,
                                          a.out_u16 ? a.out_u16 + row : nullptr,
+                                         a.out_pow ? a.out_pow + row : nullptr,
+                                         a.pair_pow ? a.pair_pow + row : nullptr,
                                          s_p,
                                          r0,
                                          N1,
@@ -529,6 +540,8 @@ cudaError_t persist_mode(const PersistArgs &a, int sms, cudaStream_t st, Persist
     case OUT_C64 | OUT_FOLD: return persist_launch<N1, N2, OUT_C64 | OUT_FOLD>(a, sms, st, plan);
     case OUT_U16 | OUT_FOLD: return persist_launch<N1, N2, OUT_U16 | OUT_FOLD>(a, sms, st, plan);
     case OUT_C64 | OUT_U16: return persist_launch<N1, N2, OUT_C64 | OUT_U16>(a, sms, st, plan);
+    case OUT_POW: return persist_launch<N1, N2, OUT_POW>(a, sms, st, plan);
+    case OUT_FOLD | OUT_PAIR: return persist_launch<N1, N2, OUT_FOLD | OUT_PAIR>(a, sms, st, plan);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -17,6 +17,8 @@ struct PersistArgs
     int out_mode;
     float2 *out_c64;
     uint32_t *out_u16;
+    float *out_pow;        // OUT_POW: |x|^2 per output sample
+    const float *pair_pow; // OUT_PAIR: the other polarisation's |a|^2, same layout
     FoldArgs fold;
     unsigned *ticket;  // zeroed before the launch
     unsigned *p1_done; // [S], zeroed before the launch

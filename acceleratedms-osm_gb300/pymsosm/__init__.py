@@ -98,6 +98,7 @@ def _declare(L):
     L.msosm_fold_dims.argtypes = [P, C.POINTER(UL), PI, C.POINTER(UL)]
     L.msosm_fold_destroy.argtypes = [P]
     L.msosm_attach_fold.argtypes = [P, P]
+    L.msosm_attach_fold_pol2.argtypes = [P, P, P]
     L.msosm_profile_enable.argtypes = [P, I]
     L.msosm_profile_reset.argtypes = [P]
     L.msosm_profile_read.argtypes = [P, I, C.POINTER(D), C.POINTER(LL), C.POINTER(LL), C.POINTER(LL)]
@@ -246,6 +247,13 @@ class MsosmGpuBatch:
     def attach_fold(self, fold: "FoldGpu | None"):
         self._check(lib().msosm_attach_fold(self._h, fold._h if fold is not None else None))
         self._fold = fold
+
+    def attach_fold_pol2(self, second: "MsosmGpuBatch", fold: "FoldGpu | None"):
+        """2-pol fused fold: this handle is the first polarisation, `second` the other;
+        each step process this one, then `second` (msosm_attach_fold_pol2)."""
+        second._check(lib().msosm_attach_fold_pol2(self._h, second._h, fold._h if fold is not None else None))
+        self._fold = fold
+        second._fold = fold
 
     # -- checkpoint / derivative -------------------------------------------
     def save_state(self, stream=None) -> np.ndarray:

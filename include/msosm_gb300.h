@@ -249,6 +249,15 @@ int msosm_fold_reset(msosm_fold_t *f, void *stream);
 int msosm_fold_dims(const msosm_fold_t *f, unsigned long *time_bin, int *num_series, unsigned long *size);
 int msosm_fold_destroy(msosm_fold_t *f);
 int msosm_attach_fold(msosm_t *h, msosm_fold_t *f);
+/* 2-pol fused fold (replaces Fold_GPU::calculate_intensity(a, b) + fold_data_phase,
+ * fold_gpu.cpp:27-60, for two processors of the same plan): `first` writes |a|^2 of
+ * every output sample into a buffer the fold owns (num_series*size floats), and every
+ * msosm_process of `second` folds sqrt(|a|^2 + |b|^2) of the same samples -- the
+ * reference's 2-pol intensity (gpu_kernel.cu:430-440) -- with no complex series written.
+ * Per step: msosm_process(first, pol_a) then msosm_process(second, pol_b) on one stream.
+ * Both handles: same DMs, batch and fftpoint (>= 65536), MSOSM_OUT_NONE. f = NULL
+ * detaches both. */
+int msosm_attach_fold_pol2(msosm_t *first, msosm_t *second, msosm_fold_t *f);
 
 /* ---- overlap-save filtering without device allocation --------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate

@@ -79,3 +79,41 @@ def test_autotune_picks_a_valid_size_and_caches(eng, tmp_path):
     assert F >= 2 * mmin and F <= 1 << 20 and (F & (F - 1)) == 0
     assert rate > 0
     assert eng.autotune(bw, f0, dms, 8, eng.IN_C64, 1 << 16, 1 << 20, 2, cache=cache) == (F, rate)
+
+
+def test_fused_two_pol_fold_matches_the_standalone_fold(eng):
+    """msosm_attach_fold_pol2 folds sqrt(|a|^2 + |b|^2) inside the second polarisation's
+    transform; it must equal the reference-shaped path (both series out, Fold_GPU's 2-pol
+    intensity) on the same int8 baseband."""
+    rng = np.random.default_rng(9)
+    bw, f0 = np.float32(32e6), np.float32(800e6)
+    dms = np.sort(rng.uniform(5.0, 60.0, 6)).astype(np.float32)
+    B, K, period, steps = 4, 256, np.float32(0.0031), 3
+    ref = [eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 16, B, eng.IN_I8, eng.OUT_C64) for _ in range(2)]
+    fus = [eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 16, B, eng.IN_I8, eng.OUT_NONE) for _ in range(2)]
+    M = ref[0].M
+    fold_ref = eng.FoldGpu(period, bw, B * M, K, len(dms))
+    fold_fus = eng.FoldGpu(period, bw, B * M, K, len(dms))
+    fus[0].attach_fold_pol2(fus[1], fold_fus)
+    for s in range(steps):
+        a = np.clip(np.round(rng.normal(0, 20, 2 * B * M)), -127, 127).astype(np.int8)
+        b = np.clip(np.round(rng.normal(0, 20, 2 * B * M)), -127, 127).astype(np.int8)
+        ref[0].filter_block(a)
+        ref[1].filter_block(b)
+        fold_ref.accumulate(ref[0].get_output_pointer(), ref[1].get_output_pointer())
+        fus[0].filter_block(a)
+        fus[1].filter_block(b)
+    _, s_ref, c_ref = fold_ref.read()
+    _, s_fus, c_fus = fold_fus.read()
+    assert int(c_fus.sum()) == len(dms) * steps * B * M
+    assert np.abs(c_fus.astype(np.int64) - c_ref.astype(np.int64)).sum() <= 2 * len(dms)
+    assert rel_l2(s_fus, s_ref) < 1e-5
+
+
+def test_fused_two_pol_fold_rejects_series_output(eng):
+    bw, f0, dms = np.float32(32e6), np.float32(800e6), [10.0, 20.0]
+    a = eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 16, 4, eng.IN_I8, eng.OUT_C64)
+    b = eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 16, 4, eng.IN_I8, eng.OUT_NONE)
+    fold = eng.FoldGpu(np.float32(0.0031), bw, 4 * a.M, 64, len(dms))
+    with pytest.raises(eng.MsosmError):
+        a.attach_fold_pol2(b, fold)
