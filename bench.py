@@ -52,13 +52,22 @@ WORKLOADS = {
                         nbins=512, samples=1 << 26, period=0.033, inject_dm=123.4, snr_db=-10.0, duty=0.05),
     "single_dm_50": dict(bw=16e6, centre=1400e6, n_dms=1, dm_lo=50.0, dm_hi=50.0, fftpoint=1 << 16, batch=32,
                          nbins=256, samples=1 << 22, period=0.033, inject_dm=50.0, snr_db=-10.0, duty=0.05),
+    # 2-pol int8 I/Q (Gaussian, sigma 20, clipped), 1024 DMs log-uniform in 1..1000 (seed 4,
+    # sorted), which forces F = 2^20; the fused 2-pol fold (msosm_attach_fold_pol2)
+    "two_pol_1024": dict(bw=128e6, centre=820e6, n_dms=1024, dm_lo=1.0, dm_hi=1000.0, dm_dist="loguniform",
+                         fftpoint=1 << 20, batch=2, nbins=256, samples=1 << 28, period=0.0071, pols=2, sigma=20.0),
 }
 
 
 def dm_grid(w, rank=0, world=1):
     if w["n_dms"] == 1:
         return np.array([w["dm_lo"]], np.float32)
-    g = np.linspace(w["dm_lo"], w["dm_hi"], w["n_dms"] * world).astype(np.float32)
+    if w.get("dm_dist") == "loguniform":
+        rng = np.random.default_rng(4)
+        g = np.sort(np.exp(rng.uniform(np.log(w["dm_lo"]), np.log(w["dm_hi"]), w["n_dms"] * world)))
+        g = g.astype(np.float32)
+    else:
+        g = np.linspace(w["dm_lo"], w["dm_hi"], w["n_dms"] * world).astype(np.float32)
     return np.ascontiguousarray(g[rank::world])
 
 
@@ -317,6 +326,118 @@ def cufft_design_rate(proc, dms, dinp, w, calls, steps, stream, engine_folded):
             "folded_rel_l2_vs_engine": diff}
 
 
+def int8_baseband(n, sigma, seed):
+    """n complex samples of int8 interleaved I/Q: N(0, sigma^2) rounded, clipped to +-127."""
+    rng = np.random.default_rng(seed)
+    out = np.empty(2 * n, np.int8)
+    step = 1 << 24
+    for i in range(0, 2 * n, step):
+        v = rng.standard_normal(min(step, 2 * n - i), dtype=np.float32) * np.float32(sigma)
+        out[i:i + len(v)] = np.clip(np.rint(v), -127, 127).astype(np.int8)
+    return out
+
+
+def run_two_pol(args, w, rank, world, local):
+    """Two polarisations of int8 baseband, every DM trial, fused 2-pol fold: per call the
+    first polarisation's transform writes |a|^2 and the second's folds sqrt(|a|^2+|b|^2)."""
+    import torch
+
+    import pymsosm as eng
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    bw, f0 = np.float32(w["bw"]), f0_of(w)
+    dms = dm_grid(w, rank, world)
+    N = w["samples"]
+    hosts = [torch.from_numpy(int8_baseband(N, w["sigma"], 40 + 2 * rank + p)).pin_memory() for p in range(2)]
+    devs = [h.to(dev) for h in hosts]
+    procs = [eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_I8, eng.OUT_NONE)
+             for _ in range(2)]
+    step_n = procs[0].batch * procs[0].M
+    calls = N // step_n
+    fold = eng.FoldGpu(np.float32(w["period"]), bw, step_n, w["nbins"], len(dms))
+    procs[0].attach_fold_pol2(procs[1], fold)
+    stream = torch.cuda.current_stream(dev)
+    bpc = 2 * step_n  # int8 bytes per call and pol
+
+    def step(src):
+        for c in range(calls):
+            procs[0].filter_block(src[0][c * bpc:(c + 1) * bpc], stream)
+            procs[1].filter_block(src[1][c * bpc:(c + 1) * bpc], stream)
+
+    for _ in range(args.warmup):
+        step(devs)
+    torch.cuda.synchronize()
+    for p in procs:
+        p.profile_reset()
+        p.profile(True)
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(devs)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    for p in procs:
+        p.profile(False)
+    t_ms = reduce_max(ev0.elapsed_time(ev1), world)
+    units_rank = 2 * N * len(dms)  # samples per pol x pols x DM trials
+    total_units = reduce_sum(units_rank * args.steps, world)
+    value = total_units / (t_ms * 1e-3)
+    profs = [p.profile_read() for p in procs]
+    launches = sum(v["launches"] for pr in profs for v in pr.values())
+    dom = "inv_persistent"
+    ms = sum(pr[dom]["ms"] for pr in profs)
+    timed = sum(pr[dom]["timed"] for pr in profs)
+    trans = sum(pr[dom]["transforms"] for pr in profs) / max(sum(pr[dom]["launches"] for pr in profs), 1)
+    per_launch_ms = ms / max(timed, 1)
+    bytes_per_launch = BYTES_PER_UNIT * procs[0].M * trans
+    peak, peak_src = measured_peak()
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": bytes_per_launch / (per_launch_ms * 1e-3) / 1e9, "peak": peak,
+        "unit": "GB/s", "frac": bytes_per_launch / (per_launch_ms * 1e-3) / 1e9 / peak, "peak_source": f"of {peak_src}",
+        "traffic": None, "bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms,
+        "pipeline_achieved": BYTES_PER_UNIT * units_rank * args.steps / (t_ms * 1e-3) / 1e9,
+    }
+    # end to end from pinned host memory, one pass over both polarisations per step
+    folded = np.zeros((len(dms), w["nbins"]), np.float32)
+    step(hosts)
+    fold.read_folded(folded, stream)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        fold.reset(stream)
+        step(hosts)
+        fold.read_folded(folded, stream)
+    torch.cuda.synchronize()
+    e_ms = reduce_max((time.perf_counter() - e0) * 1e3, world)
+    e2e = {"value": total_units / (e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(2 * hosts[0].numel()),
+           "d2h_bytes_per_step": int(folded.nbytes)}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "dm_trials_per_gpu": len(dms), "pols": 2, "fft_size": procs[0].fftpoint,
+                   "M": procs[0].M, "batch": procs[0].batch, "samples_per_pol": N, "phase_bins": w["nbins"],
+                   "bandwidth_hz": float(bw), "f0_hz": float(f0), "input": "int8 I/Q, 2 pols",
+                   "l2": "inputs larger than L2 (2 x 512 MB baseband, 2 x 8 GB responses)",
+                   "parallelism": f"dm-shard x{world}"},
+        "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+        "check": {"folded_finite": bool(np.isfinite(folded).all()), "dm_range": [float(dms[0]), float(dms[-1])]},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        rate, sec, desc, cores, _ = cpu_port_rate(w, 16, 2)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": desc + ", one polarisation (the per-pol cost of the 2-pol path)"}
+    print(json.dumps(line))
+
+
 def run_engine(args, w, rank, world, local):
     import torch
 
@@ -464,6 +585,8 @@ def main():
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, w, rank, world)
+    elif w.get("pols", 1) == 2:
+        run_two_pol(args, w, rank, world, local)
     else:
         run_engine(args, w, rank, world, local)
     if world > 1:

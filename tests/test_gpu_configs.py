@@ -4,7 +4,8 @@ Shape of the configuration: 2-pol psrdada-style int8 I/Q baseband (Gaussian,
 sigma 20, clipped to [-127, 127]), 128 MHz at 820 MHz centre, DMs log-uniform in
 1..1000 (sorted), which forces F = 2^20 (M_min of DM ~1000 is 2^19).  Here: 2^22
 samples per pol and 48 of the trials, so the FP64 oracle can follow; the engine
-runs both pols through the int8 path and folds sqrt(|a|^2+|b|^2) per DM.
+runs both pols through the int8 path and folds sqrt(|a|^2+|b|^2) per DM, both as the
+reference does (series out, then the 2-pol fold) and fused (msosm_attach_fold_pol2).
 """
 from __future__ import annotations
 
@@ -29,12 +30,15 @@ def test_two_pol_int8_f2_20(eng, orc):
         iq = np.clip(np.round(rng.normal(0.0, 20.0, 2 * N)), -127, 127).astype(np.int8)
         pols.append(iq)
     ms = [eng.MsosmGpuBatch(bw, dms, f0).initialize(0, B, eng.IN_I8, eng.OUT_C64) for _ in range(2)]
+    fus = [eng.MsosmGpuBatch(bw, dms, f0).initialize(0, B, eng.IN_I8, eng.OUT_NONE) for _ in range(2)]
     assert ms[0].fftpoint == 1 << 20 and ms[0].M == 1 << 19
     plan = orc.Plan(bw, f0, dms, 0, batch=B)
     assert plan.M == ms[0].M and plan.delaycount == ms[0].delaycount
     step = B * ms[0].M
     K, period = 256, np.float32(0.0071)
     fold = eng.FoldGpu(period, bw, step, K, len(dms))
+    fold_fus = eng.FoldGpu(period, bw, step, K, len(dms))
+    fus[0].attach_fold_pol2(fus[1], fold_fus)
     pick = [0, len(dms) // 2, len(dms) - 1]
     om = [orc.Msosm(orc.Plan(bw, f0, dms[pick], 1 << 20, batch=B), B, fp64=True) for _ in range(2)]
     got = [[], []]
@@ -49,6 +53,8 @@ def test_two_pol_int8_f2_20(eng, orc):
             got[p].append(o[pick])
             ref[p].append(om[p].process(orc.decode_i8(chunk)))
         fold.accumulate(ms[0].get_output_pointer(), ms[1].get_output_pointer())
+        for p in range(2):
+            fus[p].filter_block(np.ascontiguousarray(pols[p][2 * s * step:2 * (s + 1) * step]))
     w = plan.delaycount + 1  # windows before the ring filled
     for p in range(2):
         g = np.concatenate(got[p], axis=1)
@@ -57,6 +63,10 @@ def test_two_pol_int8_f2_20(eng, orc):
             assert rel_l2(g[k, w:], r[k, w:]) < 1e-4
     folded, sums, cnts = fold.read()
     assert cnts.sum() > 0 and np.isfinite(folded).all()
+    # the fused 2-pol fold (no series written) folds the same intensities
+    _, fsums, fcnts = fold_fus.read()
+    assert np.abs(fcnts.astype(np.int64) - cnts.astype(np.int64)).sum() <= 2 * len(dms)
+    assert rel_l2(fsums, sums) < 1e-5
     # the 2-pol fold of the picked trials equals folding the engine's own series
     dt = 1.0 / float(bw)
     for k, d in enumerate(pick):
