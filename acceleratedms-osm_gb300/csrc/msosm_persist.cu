@@ -513,10 +513,11 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     if (plan)
     {
         // Enough look-behind that items in flight rarely wait: every CTA holds its
-        // current ticket and the next one.  P2(f) sits LAG blocks after P1(f); a
-        // slot is reused S blocks later, so P1(f) waits on P2(f-S), S-LAG blocks
-        // back: S = 2*LAG keeps both distances at LAG.
-        plan->lag = 2 * ((grid + per_block - 1) / per_block) + 2;
+        // current ticket and the next one, 2*grid items = 2*grid/per_block blocks in
+        // flight.  P2(f) sits LAG blocks after P1(f); a slot is reused S blocks later,
+        // so P1(f) waits on P2(f-S), S-LAG blocks back: S = 2*LAG keeps both distances
+        // at LAG.  No more slack than that: at F = 2^20 a slot is 8 MB of L2.
+        plan->lag = (2 * grid + per_block - 1) / per_block + 1;
         plan->slots = 2 * plan->lag;
         plan->grid = grid;
         return cudaSuccess;
