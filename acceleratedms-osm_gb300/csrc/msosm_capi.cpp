@@ -549,10 +549,10 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
         cudaGetDevice(&dev);
         if ((e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
             return h->release(), h->cuda_fail(e, "cudaDeviceGetAttribute");
-        // at most 4 CTAs of 512 threads fit an SM, each holding two tickets; the
-        // kernel plans lag = 2*ceil(grid/items per transform) + 2 and 2*lag slots
+        // an upper bound of the kernel's plan (lag = ceil(2*grid/items per transform)
+        // + 1, 2*lag slots) for any grid up to 4 CTAs per SM
         const int per_block = (int)(2 * F / 8192);
-        const int lag_max = 2 * ((4 * h->sms + per_block - 1) / per_block) + 2;
+        const int lag_max = (2 * 4 * h->sms + per_block - 1) / per_block + 1;
         const int slots = std::min(kMaxSlots, 2 * lag_max);
         h->T_slots = std::max(batch, slots);
         if ((e = dalloc(&h->d_sync, (size_t)1 + 2 * kMaxSlots)) != cudaSuccess)
