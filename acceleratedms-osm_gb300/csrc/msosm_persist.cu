@@ -98,16 +98,6 @@ struct PInvLoader
     const float2 *Hd;
     const uint16_t *dl;
     int c0, N1, F, fbs, rb;
-    __device__ __forceinline__ float2 load(int col, int n2) const
-    {
-        const int n = c0 + col + N1 * n2;
-        int slot = rb - (int)__ldg(dl + n);
-        if (slot < 0)
-            slot += fbs;
-        const float2 s = __ldcs(ring + (size_t)slot * F + n);
-        const float2 h = __ldg(Hd + n);
-        return cmul(s, h);
-    }
     // The first stage's inputs in two waves: every delay, then every spectrum and
     // response value, so the delay -> spectrum dependences overlap across elements.
     template <int BPT, int R, int STRIDE, int COLS, int THREADS>
@@ -152,12 +142,6 @@ struct PStoreT
     int c0, N2;
     unsigned n2_mask;
     int n2_shift;
-    __device__ __forceinline__ void store(int col, int k2, float2 v) const
-    {
-        const int n1 = c0 + col;
-        const float2 w = twiddle_F(lo, hi, (unsigned)(n1 * k2), n2_mask, n2_shift);
-        T[(size_t)n1 * N2 + k2] = cmul(v, w);
-    }
     // Last stage: outputs k2 = base + r*Ns.  W_F^(n1*k2) = W_F^(n1*base) * (W_F^(n1*Ns))^r,
     // two table lookups per butterfly and a product chain instead of two per output.
     template <int R, int Ns>
@@ -182,10 +166,6 @@ struct PTLoader
 {
     const float2 *Ts;
     int r0, N2;
-    __device__ __forceinline__ float2 load(int col, int n1) const
-    {
-        return __ldcg(Ts + (size_t)n1 * N2 + r0 + col);
-    }
     template <int BPT, int R, int STRIDE, int COLS, int THREADS>
     __device__ __forceinline__ void load_stage(float2 (&v)[BPT][R]) const
     {
@@ -201,9 +181,9 @@ struct PTLoader
     }
 };
 
+// Placeholder first-stage source of a pass whose first stage reads shared memory.
 struct PNoLoad
 {
-    __device__ __forceinline__ float2 load(int, int) const { return make_float2(0.f, 0.f); }
 };
 
 // Last pass-2 stage: outputs k1 = base + r*Ns of row (r0 + col); only k1 >= N1/2
