@@ -574,6 +574,7 @@ def main():
                     help="skip timing the cuFFT restatement of the reference's GPU design")
     ap.add_argument("--samples", type=int, default=0, help="override the baseband length (profiling captures)")
     ap.add_argument("--dm-trials", type=int, default=0, help="override the DM-trial count (profiling captures)")
+    ap.add_argument("--batch", type=int, default=0, help="override the windows per call")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -582,6 +583,8 @@ def main():
         w["samples"] = args.samples
     if args.dm_trials:
         w["n_dms"] = args.dm_trials
+    if args.batch:
+        w["batch"] = args.batch
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, w, rank, world)
