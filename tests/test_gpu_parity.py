@@ -307,3 +307,22 @@ def test_c2_full_size(eng, orc, golden_plans):
     s_all = np.array([snr(p) for p in prof_all])
     assert s_all[pick[1]] > 3 * s_all[0]
     assert abs(float(dms[int(np.argmax(s_all))]) - 123.4) < 10.0
+
+
+def test_linearity_at_full_size(eng):
+    """Size-independent property at the many-DM workload's F = 2^18: the streaming filter
+    is linear in its input (zero-initialised state included), for every DM trial."""
+    bw, f0 = np.float32(64e6), np.float32(1368e6)
+    dms = [50.0, 123.4, 200.0]
+    B, steps = 8, 3
+    rng = np.random.default_rng(17)
+    runs = []
+    xs = [[(rng.standard_normal(B << 17) + 1j * rng.standard_normal(B << 17)).astype(np.complex64)
+           for _ in range(steps)] for _ in range(2)]
+    combo = [(2.0 * a - 3.0 * b).astype(np.complex64) for a, b in zip(*xs)]
+    for chunks in (xs[0], xs[1], combo):
+        m = _engine(eng, bw, f0, dms, 1 << 18, B, eng.IN_C64)
+        runs.append(np.concatenate(_run_engine(m, chunks), axis=1))
+    expect = 2.0 * runs[0].astype(np.complex128) - 3.0 * runs[1].astype(np.complex128)
+    for d in range(len(dms)):
+        assert rel_l2(runs[2][d], expect[d]) < 1e-5
