@@ -45,7 +45,7 @@ sys.path.insert(0, str(ROOT / "acceleratedms-osm_gb300"))
 
 METRIC = "baseband samples/s x DM trials"
 UNIT = "sample*DM/s"
-BYTES_PER_UNIT = 16  # algorithmic bytes per sample x DM (fold-only), see the design doc
+BYTES_PER_UNIT = 16  # algorithmic bytes per sample x DM, fold-only: the spectra read once per trial
 
 WORKLOADS = {
     "many_dm_512": dict(bw=64e6, centre=1400e6, n_dms=512, dm_lo=0.0, dm_hi=200.0, fftpoint=1 << 18, batch=32,
