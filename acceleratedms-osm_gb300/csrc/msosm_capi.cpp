@@ -236,7 +236,11 @@ struct msosm_s
     int T_cap = 0;
     float2 *d_tail[2] = {nullptr, nullptr};
     int tail_cur = 0;
-    void *d_in = nullptr;
+    void *d_in = nullptr;  // host-input staging, two buffers: the copy of call s+1
+    void *d_in2 = nullptr; // overlaps the transforms of call s (the reference's stream mode)
+    cudaStream_t copy_st = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
+    int in_buf = 0;
     float2 *d_out_c64 = nullptr;
     uint32_t *d_out_u16 = nullptr;
     float2 *d_tw = nullptr;
@@ -273,7 +277,22 @@ struct msosm_s
         dfree(d_T);
         dfree(d_tail[0]);
         dfree(d_tail[1]);
+        if (copy_st)
+            cudaStreamSynchronize(copy_st);
         dfree(d_in);
+        dfree(d_in2);
+        for (int i = 0; i < 2; i++)
+        {
+            if (ev_copied[i])
+                cudaEventDestroy(ev_copied[i]);
+            if (ev_consumed[i])
+                cudaEventDestroy(ev_consumed[i]);
+            ev_copied[i] = ev_consumed[i] = nullptr;
+        }
+        if (copy_st)
+            cudaStreamDestroy(copy_st);
+        copy_st = nullptr;
+        in_buf = 0;
         dfree(d_out_c64);
         dfree(d_out_u16);
         dfree(d_tw);
@@ -284,7 +303,7 @@ struct msosm_s
         d_ring = d_H = d_T = d_out_c64 = d_tw = nullptr;
         d_tail[0] = d_tail[1] = nullptr;
         d_delays = nullptr;
-        d_in = nullptr;
+        d_in = d_in2 = nullptr;
         d_out_u16 = nullptr;
         inited = false;
     }
@@ -572,8 +591,14 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
             return h->release(), h->cuda_fail(e, "cudaMemset(tail)");
     }
     const size_t in_bytes = (size_t)batch * M * in_elem_bytes(in_format);
-    if ((e = cudaMalloc(&h->d_in, in_bytes)) != cudaSuccess)
+    if ((e = cudaMalloc(&h->d_in, in_bytes)) != cudaSuccess || (e = cudaMalloc(&h->d_in2, in_bytes)) != cudaSuccess)
         return h->release(), h->cuda_fail(e, "cudaMalloc(input)");
+    if ((e = cudaStreamCreateWithFlags(&h->copy_st, cudaStreamNonBlocking)) != cudaSuccess)
+        return h->release(), h->cuda_fail(e, "cudaStreamCreate(copy)");
+    for (int i = 0; i < 2; i++)
+        if ((e = cudaEventCreateWithFlags(&h->ev_copied[i], cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&h->ev_consumed[i], cudaEventDisableTiming)) != cudaSuccess)
+            return h->release(), h->cuda_fail(e, "cudaEventCreate(copy)");
     const size_t out_elems = (size_t)h->D * batch * M;
     if (out_mode & MSOSM_OUT_C64)
         if ((e = dalloc(&h->d_out_c64, out_elems)) != cudaSuccess)
@@ -675,11 +700,19 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     const size_t in_bytes = (size_t)h->B * h->M * in_elem_bytes(h->in_format);
     const void *src = in;
     cudaError_t e;
+    const int k = h->in_buf;
     if (!in_on_device)
     {
-        if ((e = cudaMemcpyAsync(h->d_in, in, in_bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        // host input: copied on the handle's copy stream into the staging buffer that the
+        // call two back has finished reading, so it overlaps the previous call's transforms
+        void *buf = k ? h->d_in2 : h->d_in;
+        h->in_buf ^= 1;
+        if ((e = cudaStreamWaitEvent(h->copy_st, h->ev_consumed[k], 0)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(buf, in, in_bytes, cudaMemcpyDefault, h->copy_st)) != cudaSuccess ||
+            (e = cudaEventRecord(h->ev_copied[k], h->copy_st)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(st, h->ev_copied[k], 0)) != cudaSuccess)
             return h->cuda_fail(e, "cudaMemcpyAsync(input)");
-        src = h->d_in;
+        src = buf;
     }
     const int rbi = (int)((h->step * h->B) % h->fbs);
     const float2 *tail = h->d_tail[h->tail_cur];
@@ -690,6 +723,8 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     pr.end(MSOSM_KERNEL_FWD_PASS1, st, h->B);
     if (e != cudaSuccess)
         return h->cuda_fail(e, "forward transform launch (pass 1)");
+    if (!in_on_device && (e = cudaEventRecord(h->ev_consumed[k], st)) != cudaSuccess) // pass 1 read the input
+        return h->cuda_fail(e, "cudaEventRecord(input)");
     pr.begin(MSOSM_KERNEL_FWD_PASS2, st);
     e = msosm::launch_forward_p2(h->g, h->tw_fwd, h->d_T, h->d_ring, rbi, h->B, st);
     pr.end(MSOSM_KERNEL_FWD_PASS2, st, h->B);
