@@ -16,6 +16,8 @@
 // ticket can always run: no deadlock whatever the residency.  Waits are
 // nevertheless bounded by %globaltimer; on timeout the kernel raises an error
 // flag, every later wait returns at once and the host reports the failure.
+#include <algorithm>
+
 #include "msosm_common.cuh"
 #include "msosm_persist.cuh"
 
@@ -468,6 +470,27 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     }
 }
 
+// Raise (never lower) this device's persisting-L2 set-aside to `bytes`, capped at the
+// device maximum, once per size.  A failure only costs the hint.
+void ensure_l2_persisting(size_t bytes)
+{
+    static size_t done[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices || done[dev] >= bytes)
+        return;
+    int maxp = 0;
+    size_t cur = 0;
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
+        cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) == cudaSuccess)
+    {
+        const size_t want = std::min((size_t)maxp, bytes);
+        if (want > cur)
+            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);
+    }
+    cudaGetLastError();
+    done[dev] = bytes;
+}
+
 template <int N1, int N2, int MODE>
 cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
 {
@@ -506,8 +529,26 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     if (a.S <= a.lag || a.g0 < 0 || a.G < 0 || a.g0 + a.G + a.lag >= (1ll << 31) ||
         (a.G + a.lag) * (long long)per_block >= (1ll << 32))
         return cudaErrorInvalidValue;
-    k<<<grid, P_THREADS, smem, st>>>(a);
-    return cudaGetLastError();
+    // the pass-1 -> pass-2 slots are re-read within a few items: ask L2 to keep them
+    // (persisting window over the slot ring; the streamed spectra and responses miss it)
+    const size_t slot_bytes = (size_t)a.S * (size_t)(N1 * N2) * sizeof(float2);
+    ensure_l2_persisting(slot_bytes);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(P_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = (void *)a.T;
+    attr[0].val.accessPolicyWindow.num_bytes = slot_bytes;
+    attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k, a);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int N1, int N2>
