@@ -11,11 +11,13 @@
 // Dependencies, through per-slot completion counters (monotone over the launch):
 //   P2(f)  needs all P1(f)              : p1_done[f mod S] >= (f/S + 1) * n1t
 //   P1(f)  needs slot f mod S released  : p2_done[f mod S] >= (f/S) * n2t
-// Every item waited on holds a smaller ticket (S > LAG), and a CTA takes a new
-// ticket only after finishing its current item, so the smallest unfinished
-// ticket can always run: no deadlock whatever the residency.  Waits are
-// nevertheless bounded by %globaltimer; on timeout the kernel raises an error
-// flag, every later wait returns at once and the host reports the failure.
+// Every item waited on holds a smaller ticket (S > LAG).  A CTA holds its current
+// item and the next ticket (fetched early to hide the atomic's latency), and starts
+// that ticket only after finishing the current item, which has a smaller ticket; so
+// the smallest unfinished ticket is always some CTA's current item, with every
+// dependence finished: no deadlock whatever the residency.  Waits are nevertheless
+// bounded by %globaltimer; on timeout the kernel raises an error flag, every later
+// wait returns at once and the host reports the failure.
 #include <algorithm>
 
 #include "msosm_common.cuh"
@@ -230,11 +232,6 @@ struct PEpilogue
     }
 };
 
-// Bin the staged tile: each thread takes runs of G consecutive time samples; a
-// run whose first and last samples share a phase bin (runs are far shorter than a
-// period, and phase is monotone within a run) is summed in registers and lands as
-// one shared atomic; other runs go sample by sample.  Zero samples are skipped as
-// foldDataPhase_kernel does.
 // One phase bin of the per-CTA accumulator: the sum and the count side by side, so
 // that the whole shared layout sits at compile-time offsets.
 struct BinAcc
@@ -243,6 +240,11 @@ struct BinAcc
     unsigned cnt;
 };
 
+// Bin the staged tile: each thread takes runs of G consecutive time samples; a
+// run whose first and last samples share a phase bin (runs are far shorter than a
+// period, and phase is monotone within a run) is summed in registers and lands as
+// one shared atomic; other runs go sample by sample.  Zero samples are skipped as
+// foldDataPhase_kernel does.
 template <int COLS, int HALF>
 __device__ __forceinline__ void fold_tile(const float *s_p, BinAcc *s_bins, uint64_t ph_b,
                                           uint64_t dphase, unsigned K, int r0, int N2)
