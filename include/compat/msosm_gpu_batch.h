@@ -45,6 +45,10 @@ class MSOSM_GPU_BATCH : public Prepare_MSOSM
     void filter_block_uint16(uint16_pair *input)
     {
         msosm_compat::check(msosm_process(h, input, nullptr), h, "filter_block_uint16");
+        // fold mode returns with the step done, as the reference's synchronous fold-mode
+        // branch does (msosm_gpu_batch.cpp:180-202), so `input` may be refilled at once
+        if (fold)
+            msosm_compat::check(msosm_sync(h, nullptr), h, "filter_block_uint16");
     }
     void get_output(uint16_pair *output) { msosm_compat::check(msosm_get_output(h, output, nullptr), h, "get_output"); }
     void synchronize() { msosm_compat::check(msosm_sync(h, nullptr), h, "synchronize"); }

@@ -99,7 +99,10 @@ int msosm_get_response(const msosm_t *h, int dm_index, float *out);
 
 /* One streaming step: B*M new samples of the init'ed format from `in` (host or
  * device pointer; host memory should be pinned for an asynchronous copy), all
- * DMs dedispersed, outputs and the attached fold updated.  Replaces
+ * DMs dedispersed, outputs and the attached fold updated.  Asynchronous: a pinned
+ * or device `in` must stay unchanged until the step is done (msosm_sync); a
+ * pageable host `in` may be reused on return.  Host inputs are copied on the
+ * handle's own stream, overlapping the previous step's transforms.  Replaces
  * MSOSM_GPU_BATCH::filter_block_uint16(uint16_pair*) (msosm_gpu_batch.h:20,
  * msosm_gpu_batch.cpp:178-236) and its complex64 / int8 variants. */
 int msosm_process(msosm_t *h, const void *in, void *stream);
