@@ -419,13 +419,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N2, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
             fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st, tw1L);
             // publish: the barrier orders every thread's stores before thread 0's
-            // gpu-scope fence (fences are cumulative), which precedes the count
+            // gpu-scope release reduction (release is cumulative) on the count
             __syncthreads();
             if (threadIdx.x == 0)
-            {
-                __threadfence();
-                atomicAdd(a.p1_done + slot, 1u);
-            }
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p1_done + slot) : "memory");
         }
         else
         {
