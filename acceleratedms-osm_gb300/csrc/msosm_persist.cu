@@ -440,8 +440,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             // thread holds its inputs, so the slot may be refilled
             SmemIO<N1, C2::COLS> io{sm};
             fft_stage<N1, C2::COLS, P_THREADS, +1, 1, false, true, true>(PTLoader{Ts, r0, N2}, io, tw2);
-            if (threadIdx.x == 0)
-                atomicAdd(a.p2_done + slot, 1u);
+            if (threadIdx.x == 0) // release: every thread's reads of the slot precede the count
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p2_done + slot) : "memory");
             const size_t row = ((size_t)d * B + b) * M;
             PEpilogue<MODE, C2::COLS> ep{a.out_c64 ? a.out_c64 + row : nullptr,
                                          a.out_u16 ? a.out_u16 + row : nullptr,
