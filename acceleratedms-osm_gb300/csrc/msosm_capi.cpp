@@ -2,14 +2,17 @@
 //
 // Host orchestration of one streaming step, mirroring
 // MSOSM_GPU_BATCH::filter_block_uint16 (dedispersion/msosm/msosm_gpu_batch.cpp:178-236):
-//   1. new samples reach the device (copied when `in` is host memory, read in
-//      place when it is device memory);
+//   1. new samples reach the device: host inputs are copied on the handle's copy
+//      stream into one of two staging buffers (overlapping the previous step's
+//      transforms), device inputs are read in place;
 //   2. forward transforms of the B overlapping windows into ring slots
 //      rbi..rbi+B-1, rbi = (step*B) mod fbs (increment_fft_output, :167-176); the
 //      decode and the tail hand-over (increment_fft_input, :153-165) are fused in;
-//   3. for every (DM, window), in chunks sized for L2: gather x response ->
-//      inverse -> discard/scale -> outputs and/or fold.
-// Everything is ordered on the caller's stream; nothing synchronises the device.
+//   3. every (DM, window): gather x response -> inverse -> discard/scale -> outputs
+//      and/or fold, as one persistent launch (F >= 2^16, msosm_persist.cu) or as
+//      pass-1/pass-2 launch pairs over chunks sized for L2 (msosm_inverse.cu).
+// The work is ordered on the caller's stream (the copy stream joins it through
+// events); nothing synchronises the device.
 #include "msosm_gb300.h"
 
 #include "msosm_kernels.cuh"
