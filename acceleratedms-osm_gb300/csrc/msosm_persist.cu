@@ -212,8 +212,13 @@ struct PEpilogue
         {
             const int k1h = base + r * Ns - (N1 >> 1);
             float2 x = v[r];
-            x.x *= scale;
-            x.y *= scale;
+            // fold-only: |x|^2 is binned unscaled and the bins take the 1/F^2 at the
+            // flush (a power of two: the same floats as scaling each sample)
+            if constexpr (MODE != OUT_FOLD)
+            {
+                x.x *= scale;
+                x.y *= scale;
+            }
             const int o = r0 + col + N2 * k1h;
             if constexpr ((MODE & OUT_C64) != 0)
                 out_c64[o] = x;
@@ -301,7 +306,7 @@ __device__ __forceinline__ void fold_tile(const float *s_p, BinAcc *s_bins, uint
 // the CTA's consecutive pass-2 items of that trial and flushed to the global
 // double / u64 sums when the trial changes and at the end.  Each thread flushes and
 // clears the bins it owns; the callers' barriers order this against fold_tile().
-__device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, int d)
+__device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, int d, double scale2)
 {
     double *gs = fa.sum + (size_t)d * fa.K;
     unsigned long long *gc = fa.cnt + (size_t)d * fa.K;
@@ -310,7 +315,7 @@ __device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, i
         const BinAcc v = s_bins[i];
         if (v.cnt)
         {
-            atomicAdd(gs + i, (double)v.sum);
+            atomicAdd(gs + i, (double)v.sum * scale2);
             atomicAdd(gc + i, (unsigned long long)v.cnt);
             s_bins[i] = BinAcc{0.0f, 0u};
         }
@@ -334,6 +339,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     // the last stage's, so the [r][k] table replaces the W_{N2} table
     constexpr bool P1_TWO = NSL == StageRadix<N2, 1, true>::value;
     constexpr bool FOLD = (MODE & OUT_FOLD) != 0;
+    // fold-only bins hold unscaled |x|^2: 1/F^2 at the flush (exact, F a power of two)
+    constexpr double FLUSH_SCALE2 = (MODE == OUT_FOLD) ? 1.0 / ((double)F * (double)F) : 1.0;
     static_assert(C2::COLS * (N1 / 2) <= 2 * DATA, "fold staging fits in the data tile");
     extern __shared__ float2 smem[];
     float2 *sm = smem;
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                 if (d != fold_d)
                 {
                     if (fold_d >= 0)
-                        fold_flush(s_bins, a.fold, fold_d);
+                        fold_flush(s_bins, a.fold, fold_d, FLUSH_SCALE2);
                     fold_d = d;
                 }
             }
@@ -465,7 +472,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     if constexpr (FOLD)
     {
         if (fold_d >= 0)
-            fold_flush(s_bins, a.fold, fold_d);
+            fold_flush(s_bins, a.fold, fold_d, FLUSH_SCALE2);
     }
 }
 
