@@ -83,3 +83,40 @@ def test_create_computes_nd_on_host(eng, golden_plans):
     # process before init is a state error, not a crash
     with pytest.raises(eng.MsosmError):
         m.filter_block(np.zeros(4, np.uint32))
+
+
+def test_header_is_plain_c_and_links(tmp_path, eng):
+    """include/msosm_gb300.h is the C boundary: strict C99 compiles against it and a C
+    program links the library and runs the host-only planning entry points."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    root = Path(__file__).resolve().parents[1]
+    lib = root / "acceleratedms-osm_gb300" / "lib"
+    src = tmp_path / "probe.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "msosm_gb300.h"
+int main(void)
+{
+    float dms[2] = {1.0f, 2.0f};
+    int nd[2] = {0, 0};
+    if (msosm_plan_nd(4e6f, 400e6f, dms, 2, nd) != MSOSM_OK)
+        return 1;
+    printf("%s %d %d\n", msosm_status_string(MSOSM_ERR_ARG), nd[0], nd[1]);
+    return 0;
+}
+""")
+    exe = tmp_path / "probe"
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(root / "include"),
+                        str(src), "-L", str(lib), "-lmsosm_gb300", f"-Wl,-rpath,{lib}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr
+    words = run.stdout.split()
+    assert int(words[-2]) > 0 and int(words[-1]) > int(words[-2])
