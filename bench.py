@@ -19,6 +19,14 @@ One "step" = one pass of the engine over the whole 2^26-sample baseband
           inside the timed region, against the measured HBM copy bandwidth.
   cpu_baseline  the FP32 CPU port of the same algorithm (oracle/) on a bounded
           sample, all host threads.
+  reference_gpu_design  the reference's GPU design (cuFFT forward, gather x
+          response, batched cuFFT inverse, discard + fold) restated in
+          baseline/cufft_pipeline and timed on the same workload (off with
+          --no-cufft-baseline).
+
+Other workloads: --workload single_dm_50 (1 DM at 16 MHz, F = 2^16) and
+--workload two_pol_1024 (2-pol int8, 1024 log-uniform DMs, F = 2^20, fused 2-pol
+fold); --samples / --dm-trials / --batch shrink or reshape a workload for captures.
 
 `--impl reference` times that CPU implementation alone (the reference has no
 CPU MS-OSM path of its own; its planning code is x86-build-only here).
