@@ -18,6 +18,7 @@
 #include "msosm_kernels.cuh"
 #include "msosm_persist.cuh"
 #include "msosm_plan.h"
+#include "msosm_tc.cuh"
 #include "msosm_writer.h"
 
 #include <cuda_runtime.h>
@@ -961,6 +962,15 @@ extern "C" int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long l
 }
 
 // ---- FFT-size autotuning ---------------------------------------------------------
+extern "C" int msosm_selftest_umma(int bf16, int n, int b_row0, const uint16_t *A, const uint16_t *B, float *D,
+                                   int *timed_out)
+{
+    if (!A || !B || !D || !timed_out || (n != 32 && n != 64) || b_row0 < 0 || b_row0 + n > 64 || b_row0 % 8)
+        return MSOSM_ERR_ARG;
+    cudaError_t e = msosm::tc_selftest_umma(bf16, n, b_row0, A, B, D, timed_out);
+    return e == cudaSuccess ? MSOSM_OK : MSOSM_ERR_CUDA;
+}
+
 extern "C" int msosm_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
                                    unsigned long long *elapsed_ns)
 {

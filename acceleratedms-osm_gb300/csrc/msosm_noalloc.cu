@@ -15,16 +15,18 @@
 // holds its 18,939,904 bytes (about 18 MiB) until the process exits.  The
 // first call on each device looks the array's device address up with
 // cudaGetSymbolAddress (a one-time set-up per device), so make that first call
-// before any stream capture begins.  All calls share the array and it keeps
-// the last call's contents, so calls whose work overlaps on the GPU (for
-// example the same or different threads issuing on two streams without
-// ordering between them) race on it; order such calls on one stream.
+// before any stream capture begins.  The looked-up address is kept for the life
+// of the process, so the entry point must not be used on a device after
+// cudaDeviceReset (which unloads the module the array lives in).  All calls
+// share the array and it keeps the last call's contents, so calls whose work
+// overlaps on the GPU (for example the same or different threads issuing on two
+// streams without ordering between them) race on it; order such calls on one
+// stream.
 #include "msosm_gb300.h"
 #include "msosm_kernels.cuh"
 
 #include <cuda_runtime.h>
 
-#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -79,39 +81,49 @@ int scratch_address(void **out)
     return MSOSM_OK;
 }
 
+// Device memory of the current device (or managed memory): anything else would
+// make the kernels reach another GPU's memory or host memory.
 bool device_pointer(const void *p)
 {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return false;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
     {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
 }
 
-// W tables for both directions, laid out as the engine's handles lay them out.
-void fill_twiddles(float2 *host, int N1, int N2, int F)
+// W tables for both directions, laid out as the engine's handles lay them out
+// (per direction: W_N1^m, W_N2^m, W_F^m for m < N2, W_F^(m*N2) for m < N1), computed
+// on the device from (N1, N2, F) in double precision and rounded once to float;
+// the same launch zeroes the delay map, since the array keeps what the last call
+// left there.
+__global__ void noalloc_setup_kernel(float2 *tw, int N1, int N2, int F, uint32_t *delay_words, int nwords)
 {
-    const double PI = 3.14159265358979323846;
-    const size_t per = (size_t)2 * N1 + 2 * N2;
-    for (int dir = 0; dir < 2; dir++)
+    const int per = 2 * N1 + 2 * N2;
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * per; i += stride)
     {
-        const double sgn = dir == 0 ? -1.0 : 1.0;
-        float2 *b = host + dir * per;
-        auto w = [&](long long m, long long n) {
-            const double a = 2.0 * PI * (double)(m % n) / (double)n;
-            return make_float2((float)std::cos(a), (float)(sgn * std::sin(a)));
-        };
-        for (int m = 0; m < N1; m++)
-            b[m] = w(m, N1);
-        for (int m = 0; m < N2; m++)
-            b[N1 + m] = w(m, N2);
-        for (int m = 0; m < N2; m++)
-            b[N1 + N2 + m] = w(m, F);
-        for (int m = 0; m < N1; m++)
-            b[N1 + 2 * N2 + m] = w((long long)m * N2, F);
+        const int dir = i / per, j = i % per;
+        long long m, n;
+        if (j < N1)
+            m = j, n = N1;
+        else if (j < N1 + N2)
+            m = j - N1, n = N2;
+        else if (j < N1 + 2 * N2)
+            m = j - N1 - N2, n = F;
+        else
+            m = (long long)(j - N1 - 2 * N2) * N2, n = F;
+        double s, c;
+        sincospi(2.0 * (double)(m % n) / (double)n, &s, &c); // exp(+-2 pi i m/n)
+        tw[i] = make_float2((float)c, (float)(dir == 0 ? -s : s));
     }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride)
+        delay_words[i] = 0u;
 }
 
 } // namespace
@@ -155,16 +167,13 @@ extern "C" int msosm_osm_filter_noalloc(const void *x, const void *H, int fftpoi
     float2 *tw_dev = reinterpret_cast<float2 *>(base + kOffTw);
     cudaStream_t st = (cudaStream_t)stream;
 
-    // twiddles: computed on the host into a fixed buffer, copied into the array
-    static thread_local float2 tw_host[kTwElems];
-    fill_twiddles(tw_host, g.N1, g.N2, F);
-    const size_t per = (size_t)2 * g.N1 + 2 * g.N2;
-    cudaError_t e = cudaMemcpyAsync(tw_dev, tw_host, 2 * per * sizeof(float2), cudaMemcpyHostToDevice, st);
-    // the delay map must read zero: the array keeps whatever the last call left
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(zero_delays, 0, (size_t)F * sizeof(uint16_t), st);
+    // twiddles of this fftpoint and a zero delay map, written into the array on `st`
+    // (nothing is read from host memory)
+    noalloc_setup_kernel<<<64, 256, 0, st>>>(tw_dev, g.N1, g.N2, F, reinterpret_cast<uint32_t *>(zero_delays), F / 2);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return MSOSM_ERR_CUDA;
+    const size_t per = (size_t)2 * g.N1 + 2 * g.N2;
     const msosm::Twiddles fwd{tw_dev, tw_dev + g.N1, tw_dev + g.N1 + g.N2, tw_dev + g.N1 + 2 * g.N2};
     const msosm::Twiddles inv{tw_dev + per, tw_dev + per + g.N1, tw_dev + per + g.N1 + g.N2,
                               tw_dev + per + g.N1 + 2 * g.N2};

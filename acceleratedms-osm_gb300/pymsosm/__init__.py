@@ -515,3 +515,24 @@ def selftest_wait(preset: int, target: int, timeout_ns: int) -> tuple[bool, int]
     if rc != OK:
         raise MsosmError(f"selftest_wait: {L.msosm_status_string(rc).decode()}")
     return bool(t.value), int(e.value)
+
+
+def selftest_umma(A: np.ndarray, B: np.ndarray, n: int = 64, b_row0: int = 0, bf16: bool = True) -> np.ndarray:
+    """Tensor-core operand-layout self-test (msosm_selftest_umma): D = A x B[b_row0:b_row0+n]^T
+    computed by tcgen05 MMAs from 16-bit operands (uint16 bit patterns, A 128 x 64, B 64 x 64)
+    with FP32 accumulation.  Returns D (128 x n float32)."""
+    L = lib()
+    L.msosm_selftest_umma.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_int)]
+    a = np.ascontiguousarray(A, dtype=np.uint16)
+    b = np.ascontiguousarray(B, dtype=np.uint16)
+    if a.shape != (128, 64) or b.shape != (64, 64):
+        raise ValueError("A must be 128 x 64 and B 64 x 64")
+    d = np.zeros((128, n), np.float32)
+    t = C.c_int()
+    rc = L.msosm_selftest_umma(int(bf16), n, b_row0, a.ctypes.data, b.ctypes.data, d.ctypes.data, C.byref(t))
+    if rc != OK:
+        raise MsosmError(f"selftest_umma: {L.msosm_status_string(rc).decode()}")
+    if t.value:
+        raise MsosmError("selftest_umma: the MMA wait timed out")
+    return d

@@ -163,6 +163,16 @@ int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch,
 int msosm_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
                         unsigned long long *elapsed_ns);
 
+/* Tensor-core operand-layout self-test (no counterpart in the reference): one CTA
+ * computes D[m][j] = sum_k A[m][k] * B[b_row0 + j][k] (m < 128, j < n, k < 64;
+ * n = 32 or 64, b_row0 a multiple of 8) with tcgen05 MMAs from shared memory in
+ * the layout the split-precision transform uses, FP32 accumulation in tensor
+ * memory.  A (128 x 64) and B (64 x 64) are row-major 16-bit host arrays, FP16 or
+ * (bf16 != 0) BF16; D is a host array of 128*n floats.  *timed_out = 1 when the
+ * kernel's bounded wait for the MMAs ran out. */
+int msosm_selftest_umma(int bf16, int n, int b_row0, const uint16_t *A, const uint16_t *B, float *D,
+                        int *timed_out);
+
 /* ---- per-DM output files -------------------------------------------------------
  * Replaces MSOSM_DataSave_Uring (data_save/include/msosm_data_save_uring.h:22-52,
  * msosm_data_save_uring.cpp:40-288) with pwrite worker threads (no liburing):
@@ -278,9 +288,12 @@ int msosm_attach_fold_pol2(msosm_t *first, msosm_t *second, msosm_fold_t *f);
  * allocating call is made.  Limits: fftpoint a power of two in [2^8, 2^20] and
  * count*fftpoint <= 2^20; larger requests return MSOSM_ERR_UNSUPPORTED with a
  * message on stderr.  The first call on each device looks up the array's device
- * address (one-time set-up), so make it before any stream capture.  All calls
- * share the array and it keeps the last call's contents: calls that overlap on
- * the GPU race, so order them on one stream. */
+ * address (one-time set-up), so make it before any stream capture.  The address
+ * is kept for the life of the process: do not use this entry point on a device
+ * after cudaDeviceReset.  x, H and out must be device memory of the current
+ * device (or managed memory).  All calls share the array and it keeps the last
+ * call's contents: calls that overlap on the GPU race, so order them on one
+ * stream. */
 int msosm_osm_filter_noalloc(const void *x, const void *H, int fftpoint, int count, void *out, void *stream);
 
 #ifdef __cplusplus
