@@ -258,6 +258,12 @@ struct msosm_s
     long long step = 0;
     msosm_fold_t *fold = nullptr;
     msosm_writer_s *writer = nullptr;
+    // split-precision transform (tensor cores): precision, W_32 operand image, FP16
+    // operand-scale bound (running max |component| of the ring) and max |H|
+    int precision = msosm::PREC_FP32;
+    void *d_tc_op = nullptr;
+    unsigned *d_absmax = nullptr;
+    float hmax = 1.0f;
     float *pair_out = nullptr;      // first polarisation of a 2-pol fused fold: |a|^2 goes here
     const float *pair_in = nullptr; // second polarisation: folds sqrt(pair_in + |b|^2)
     Profiler prof;
@@ -302,6 +308,11 @@ struct msosm_s
         dfree(d_tw);
         dfree(d_sync);
         dfree(d_err);
+        dfree(d_tc_op);
+        dfree(d_absmax);
+        d_tc_op = nullptr;
+        d_absmax = nullptr;
+        precision = msosm::PREC_FP32;
         d_sync = nullptr;
         d_err = nullptr;
         d_ring = d_H = d_T = d_out_c64 = d_tw = nullptr;
@@ -436,6 +447,15 @@ extern "C" int osm_create(float bw, float dm, float f0, msosm_t **out)
     return MSOSM_OK;
 }
 
+// Largest |H| over interleaved (re, im) floats.
+static float max_abs_complex(const std::vector<float> &H)
+{
+    double m = 0;
+    for (size_t i = 0; i + 1 < H.size(); i += 2)
+        m = std::max(m, std::hypot((double)H[i], (double)H[i + 1]));
+    return (float)m;
+}
+
 static int build_twiddles(msosm_t *h)
 {
     const int N1 = h->g.N1, N2 = h->g.N2, F = h->g.F;
@@ -546,6 +566,7 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
     std::vector<float> H(2 * DF);
     const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
     msosm::plan_responses(h->bw, h->f0, h->dms.data(), h->D, M, H.data(), threads);
+    h->hmax = max_abs_complex(H);
 
     cudaError_t e;
     const size_t ring_elems = (size_t)h->fbs * F;
@@ -617,6 +638,41 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
     h->tail_cur = 0;
     h->inited = true;
     return MSOSM_OK;
+}
+
+extern "C" int msosm_set_precision(msosm_t *h, int precision)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "set_precision before init");
+    if (precision != MSOSM_PREC_FP32 && precision != MSOSM_PREC_BF16X3 && precision != MSOSM_PREC_FP16X3)
+        return h->fail(MSOSM_ERR_ARG, "unknown precision");
+    if (precision == MSOSM_PREC_FP32)
+    {
+        h->precision = msosm::PREC_FP32;
+        return MSOSM_OK;
+    }
+    if (!h->persist || !msosm::tc_supported(h->g.L))
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "the split-precision transform is built for fftpoint 2^18 only");
+    cudaError_t e;
+    if (!h->d_tc_op && (e = cudaMalloc(&h->d_tc_op, 16384)) != cudaSuccess)
+        return h->cuda_fail(e, "cudaMalloc(tensor-core operand)");
+    if (!h->d_absmax && (e = dalloc(&h->d_absmax, 1)) != cudaSuccess)
+        return h->cuda_fail(e, "cudaMalloc(spectra bound)");
+    // the operand image and a bound covering every spectrum already in the ring
+    if ((e = msosm::tc_build_operand(h->d_tc_op, precision == MSOSM_PREC_BF16X3, nullptr)) != cudaSuccess ||
+        (e = cudaMemset(h->d_absmax, 0, sizeof(unsigned))) != cudaSuccess ||
+        (e = msosm::tc_absmax(h->d_ring, (size_t)h->fbs * h->F, h->d_absmax, nullptr)) != cudaSuccess ||
+        (e = cudaDeviceSynchronize()) != cudaSuccess)
+        return h->cuda_fail(e, "set_precision");
+    h->precision = precision == MSOSM_PREC_BF16X3 ? msosm::PREC_BF16X3 : msosm::PREC_FP16X3;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_get_precision(const msosm_t *h)
+{
+    return h ? h->precision : -1;
 }
 
 extern "C" int msosm_get_dims(const msosm_t *h, int *M, int *M_min, int *fftpoint, int *batch, int *num_dms,
@@ -734,6 +790,9 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     pr.end(MSOSM_KERNEL_FWD_PASS2, st, h->B);
     if (e != cudaSuccess)
         return h->cuda_fail(e, "forward transform launch (pass 2)");
+    if (h->precision == msosm::PREC_FP16X3 &&
+        (e = msosm::tc_absmax(h->d_ring + (size_t)rbi * h->F, (size_t)h->B * h->F, h->d_absmax, st)) != cudaSuccess)
+        return h->cuda_fail(e, "spectra bound launch");
 
     msosm::InvArgs a{};
     a.ring = h->d_ring;
@@ -784,8 +843,11 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         pa.p2_done = h->d_sync + 1 + kMaxSlots;
         pa.err = h->d_err;
         pa.timeout_ns = kWaitTimeoutNs;
+        msosm::TcArgs tc{static_cast<const uint4 *>(h->d_tc_op), h->d_absmax, h->hmax};
+        const bool use_tc = h->precision != msosm::PREC_FP32;
         msosm::PersistPlan plan;
-        e = msosm::persist_plan(h->g.L, pa, h->sms, &plan);
+        e = use_tc ? msosm::tc_plan(h->g.L, h->precision, pa, tc, h->sms, &plan)
+                   : msosm::persist_plan(h->g.L, pa, h->sms, &plan);
         if (e != cudaSuccess)
             return h->cuda_fail(e, "persistent transform plan");
         pa.lag = plan.lag;
@@ -795,7 +857,8 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         if ((e = cudaMemsetAsync(h->d_sync, 0, sizeof(unsigned) * (1 + 2 * kMaxSlots), st)) != cudaSuccess)
             return h->cuda_fail(e, "cudaMemsetAsync(sync)");
         pr.begin(MSOSM_KERNEL_INV_FUSED, st);
-        e = msosm::launch_inverse_persistent(h->g.L, pa, h->sms, st);
+        e = use_tc ? msosm::launch_inverse_tc(h->g.L, h->precision, pa, tc, h->sms, st)
+                   : msosm::launch_inverse_persistent(h->g.L, pa, h->sms, st);
         pr.end(MSOSM_KERNEL_INV_FUSED, st, total);
         if (e != cudaSuccess)
             return h->cuda_fail(e, "persistent inverse transform launch");
@@ -1082,6 +1145,7 @@ extern "C" int msosm_use_response_derivative(msosm_t *h)
     std::vector<float> H(2 * DF);
     const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
     msosm::plan_responses(h->bw, h->f0, h->dms.data(), h->D, h->M, H.data(), threads, true);
+    h->hmax = max_abs_complex(H);
     cudaError_t e = cudaMemcpy(h->d_H, H.data(), DF * sizeof(float2), cudaMemcpyHostToDevice);
     return e == cudaSuccess ? MSOSM_OK : h->cuda_fail(e, "cudaMemcpy(dH)");
 }
@@ -1182,6 +1246,14 @@ extern "C" int msosm_load_state(msosm_t *h, const void *buf, size_t bytes, void 
     if (e != cudaSuccess)
         return h->cuda_fail(e, "load_state");
     h->step = hd.step;
+    if (h->precision == msosm::PREC_FP16X3)
+    {
+        // the operand-scale bound must cover the loaded ring
+        if ((e = cudaMemsetAsync(h->d_absmax, 0, sizeof(unsigned), st)) != cudaSuccess ||
+            (e = msosm::tc_absmax(h->d_ring, (size_t)h->fbs * h->F, h->d_absmax, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            return h->cuda_fail(e, "load_state (spectra bound)");
+    }
     return MSOSM_OK;
 }
 

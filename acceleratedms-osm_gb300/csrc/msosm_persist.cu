@@ -20,8 +20,12 @@
 // wait returns at once and the host reports the failure.
 #include <algorithm>
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "msosm_common.cuh"
 #include "msosm_persist.cuh"
+#include "umma.cuh"
 
 namespace msosm {
 
@@ -322,6 +326,33 @@ __device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, i
     }
 }
 
+// Thread 0 of a CTA: take the ticket it holds (fetching the next one, whose latency
+// overlaps the item), wait for the item's dependences, and return the verdict:
+// -1 stop (tickets exhausted; or, with stop_on_error, the launch failed), 0 skip
+// (outside the launch's transforms, or a failed wait), 1 run.
+template <int n1t, int n2t>
+__device__ __forceinline__ int judge_ticket(const PersistArgs &a, long long total, unsigned &held, unsigned &t_out,
+                                            bool stop_on_error)
+{
+    constexpr int per_block = n1t + n2t;
+    const unsigned t = held;
+    t_out = t;
+    if ((long long)t >= total || (stop_on_error && *(volatile int *)a.err))
+        return -1;
+    held = atomicAdd(a.ticket, 1u);
+    const long long q = t / per_block;
+    const int w = (int)(t % per_block);
+    const bool p1 = w < n1t;
+    const long long f = p1 ? q : q - a.lag;
+    if (f < 0 || f >= a.G)
+        return 0;
+    const unsigned slot = (unsigned)f % (unsigned)a.S; // f < 2^31 (host check)
+    const unsigned gen = (unsigned)f / (unsigned)a.S;
+    const bool ok = p1 ? wait_count(a.p2_done + slot, gen * n2t, a.err, a.timeout_ns)
+                       : wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, a.timeout_ns);
+    return ok ? 1 : 0;
+}
+
 template <int N1, int N2, int MODE>
 __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArgs a)
 {
@@ -382,27 +413,9 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         const int par = it & 1;
         if (threadIdx.x == 0)
         {
-            const unsigned t = held;
-            int verdict = -1; // -1 stop, 0 skip, 1 run
-            if ((long long)t < total)
-            {
-                held = atomicAdd(a.ticket, 1u); // its latency overlaps this item
-                const long long q = t / per_block;
-                const int w = (int)(t % per_block);
-                const bool p1 = w < n1t;
-                const long long f = p1 ? q : q - a.lag;
-                verdict = 0;
-                if (f >= 0 && f < a.G)
-                {
-                    const unsigned slot = (unsigned)f % (unsigned)a.S; // f < 2^31 (host check)
-                    const unsigned gen = (unsigned)f / (unsigned)a.S;
-                    const bool ok = p1 ? wait_count(a.p2_done + slot, gen * n2t, a.err, a.timeout_ns)
-                                       : wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, a.timeout_ns);
-                    verdict = ok ? 1 : 0;
-                }
-            }
+            unsigned t;
+            s_verdict[par] = judge_ticket<n1t, n2t>(a, total, held, t, false);
             s_ticket[par] = t;
-            s_verdict[par] = verdict;
         }
         __syncthreads(); // also fences the previous item's shared-memory use
         const int verdict = s_verdict[par];
@@ -476,6 +489,356 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     }
 }
 
+// ---- split-precision transform on the tensor cores --------------------------------
+// F = 2^18 (N1 = N2 = 512).  Each 512-point DFT of a pass is split as n = 32a + b,
+// k = ka + 16*kb:
+//   step 1 (registers): y[b][ka] = sum_a x[32a + b] W_16^(a*ka), z = y * W_512^(b*ka)
+//   step 2 (tensor cores): X[ka + 16*kb] = sum_b z[b][ka] W_32^(b*kb)
+// Step 2 is a real GEMM per item of 16 vectors: A rows m = 16*ka + v (two 128-row
+// tiles), K = (b, re/im) = 64, B = the real 64 x 64 form of W_32, D = 64 (pass 1)
+// or the 32 kept columns kb >= 16 (pass 2: only outputs k1 >= 256 survive the
+// discard).  FP32 values are split into 16-bit hi + lo parts (BF16 or FP16) and
+// D = Ahi*Bhi + Alo*Bhi + Ahi*Blo accumulates in FP32 in tensor memory: 24 MMAs of
+// 128 x N x 16 per item.  FP16 operands are scaled by powers of two chosen from a
+// running bound on the spectra so that no value exceeds the FP16 range; the scale is
+// taken back out in FP32 afterwards (exact).
+//
+// The pass-1 -> pass-2 slot is row-major here: element (k2, n1) at k2*512 + n1.
+// Shared memory (1024-byte aligned base): A hi tiles (2 x 16 KB), A lo tiles, B hi
+// (8 KB), B lo, the step-1 twiddle tables of both passes W[ka][i][bp] =
+// W_512^((2bp+i)*ka) * scale (4 KB each), fold bins.  Fold staging reuses the A tiles
+// once an item's MMAs are done.
+constexpr int TC_N = 512;                  // sub-transform length of both passes
+constexpr int TC_COLS = 16;                // vectors per item
+constexpr uint32_t TC_A_HI = 0;            // two 128-row tiles, 16 KB each
+constexpr uint32_t TC_A_LO = 32768;
+constexpr uint32_t TC_B_HI = 65536;        // 64 rows x 128 B
+constexpr uint32_t TC_B_LO = 73728;
+constexpr uint32_t TC_W1 = 81920;          // 512 float2
+constexpr uint32_t TC_W2 = 86016;
+constexpr uint32_t TC_BINS = 90112;
+constexpr uint32_t TC_TMEM_COLS = 128;     // two 64-column FP32 accumulator tiles
+
+template <bool BF16>
+__device__ __forceinline__ void split_hi_lo(float2 z, uint32_t &hi, uint32_t &lo)
+{
+    if constexpr (BF16)
+    {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(z.x, z.y);
+        const float2 hf = __bfloat1622float2(h);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(z.x - hf.x, z.y - hf.y);
+        hi = *reinterpret_cast<const uint32_t *>(&h);
+        lo = *reinterpret_cast<const uint32_t *>(&l);
+    }
+    else
+    {
+        const __half2 h = __floats2half2_rn(z.x, z.y);
+        const float2 hf = __half22float2(h);
+        const __half2 l = __floats2half2_rn(z.x - hf.x, z.y - hf.y);
+        hi = *reinterpret_cast<const uint32_t *>(&h);
+        lo = *reinterpret_cast<const uint32_t *>(&l);
+    }
+}
+
+// Step 1 of either pass for this thread's two vectors' columns b = 2bp, 2bp+1:
+// 16-point DFTs over a, twiddles from W[ka][i][bp], hi/lo split, stored as A rows
+// m = 16*ka + v at K = 4bp .. 4bp+3 (row_off: this thread's byte offset in row v of
+// tile 0; row m lands at tile ka/8, 2048*(ka%8) bytes further).
+template <bool BF16>
+__device__ __forceinline__ void tc_step1(float2 (&x)[2][16], const float2 *__restrict__ W, int bp, uint32_t row_off,
+                                         unsigned char *sA_hi, unsigned char *sA_lo)
+{
+    dftR<16, +1>(x[0]);
+    dftR<16, +1>(x[1]);
+#pragma unroll
+    for (int ka = 0; ka < 16; ka++)
+    {
+        const float2 z0 = cmul(x[0][ka], W[ka * 32 + bp]);
+        const float2 z1 = cmul(x[1][ka], W[ka * 32 + 16 + bp]);
+        uint32_t h0, l0, h1, l1;
+        split_hi_lo<BF16>(z0, h0, l0);
+        split_hi_lo<BF16>(z1, h1, l1);
+        const uint32_t off = (uint32_t)(ka >> 3) * 16384u + (uint32_t)(ka & 7) * 2048u + row_off;
+        *reinterpret_cast<uint2 *>(sA_hi + off) = make_uint2(h0, h1);
+        *reinterpret_cast<uint2 *>(sA_lo + off) = make_uint2(l0, l1);
+    }
+}
+
+// Thread 0: the 24 MMAs of one item (two A tiles x three products x four K-steps),
+// then a commit that completes the mbarrier's phase when they are done.
+__device__ __forceinline__ void tc_issue(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
+                                         uint32_t idesc, uint64_t *mbar)
+{
+    umma::fence_after_sync();
+#pragma unroll
+    for (int t = 0; t < 2; t++)
+    {
+        const uint32_t d = tmem + 64u * t;
+        const uint32_t ah = a_hi + 16384u * t, al = a_lo + 16384u * t;
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++)
+            umma::mma_f16(d, umma::desc_sw128(ah + 32u * ks), umma::desc_sw128(b_hi + 32u * ks), idesc, ks > 0);
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++)
+            umma::mma_f16(d, umma::desc_sw128(al + 32u * ks), umma::desc_sw128(b_hi + 32u * ks), idesc, 1u);
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++)
+            umma::mma_f16(d, umma::desc_sw128(ah + 32u * ks), umma::desc_sw128(b_lo + 32u * ks), idesc, 1u);
+    }
+    umma::commit(mbar);
+}
+
+template <int MODE, bool BF16>
+__global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcArgs tc)
+{
+    constexpr int N1 = TC_N, N2 = TC_N, F = N1 * N2, M = F / 2;
+    constexpr int n1t = N1 / TC_COLS, n2t = N2 / TC_COLS, per_block = n1t + n2t;
+    constexpr bool FOLD = (MODE & OUT_FOLD) != 0;
+    constexpr uint32_t IDESC_P1 = umma::idesc_f16(128, 64, BF16);
+    constexpr uint32_t IDESC_P2 = umma::idesc_f16(128, 32, BF16);
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ unsigned s_ticket[2];
+    __shared__ int s_verdict[2];
+    const uint32_t pad = (1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u;
+    unsigned char *base = smem_raw + pad;
+    unsigned char *sA_hi = base + TC_A_HI, *sA_lo = base + TC_A_LO;
+    float2 *W1 = reinterpret_cast<float2 *>(base + TC_W1);
+    float2 *W2 = reinterpret_cast<float2 *>(base + TC_W2);
+    BinAcc *s_bins = reinterpret_cast<BinAcc *>(base + TC_BINS);
+    float *s_p = reinterpret_cast<float *>(base + TC_A_HI); // fold staging, 16 KB
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    // operand scales (powers of two): FP16 keeps every operand below 2^15
+    float s1 = 1.0f, s2 = 1.0f;
+    if constexpr (!BF16)
+    {
+        const float mx = __uint_as_float(__ldcg(tc.absmax)) * tc.hmax * 1.41421357f; // max |X*H|
+        if (mx > 0.0f && mx < 1e30f)
+        {
+            // step-1 outputs are at most 16*mx (pass 1) and 16*512*mx (pass 2)
+            s1 = ldexpf(1.0f, min(100, max(-100, 14 - ilogbf(16.0f * mx))));
+            s2 = ldexpf(1.0f, min(100, max(-100, 14 - ilogbf(8192.0f * mx))));
+        }
+    }
+    // the W_32 operand image (hi then lo, already in the swizzled layout)
+    for (int i = tid; i < 1024; i += P_THREADS)
+        reinterpret_cast<uint4 *>(base + TC_B_HI)[i] = __ldg(tc.bop + i);
+    for (int e = tid; e < 512; e += P_THREADS)
+    {
+        const int ka = e >> 5, i = (e >> 4) & 1, bp = e & 15;
+        const float2 w = __ldg(a.tw.twN1 + (2 * bp + i) * ka); // (2bp+i)*ka < 512
+        W1[e] = make_float2(w.x * s1, w.y * s1);
+        W2[e] = make_float2(w.x * s2, w.y * s2);
+    }
+    if constexpr (FOLD)
+    {
+        for (unsigned i = tid; i < a.fold.K; i += P_THREADS)
+            s_bins[i] = BinAcc{0.0f, 0u};
+    }
+    if (warp == 0)
+        umma::tmem_alloc(&tmem_slot, TC_TMEM_COLS);
+    if (tid == 0)
+        umma::mbar_init(&mbar, 1);
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t a_hi = umma::smem_addr(sA_hi), a_lo = umma::smem_addr(sA_lo);
+    const uint32_t b_hi = umma::smem_addr(base + TC_B_HI), b_lo = umma::smem_addr(base + TC_B_LO);
+    // this thread's accumulator row: tile t = warp/4, TMEM lanes of quarter warp%4
+    const int acc_t = warp >> 2, acc_m = 32 * (warp & 3) + lane;
+    const int acc_ka = 8 * acc_t + (acc_m >> 4), acc_v = acc_m & 15;
+    const uint32_t acc_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 64u * acc_t;
+    const float inv_s1 = 1.0f / s1;
+    const float out_scale = 1.0f / (s2 * (float)F);
+    const double flush_scale2 = (MODE == OUT_FOLD) ? 1.0 / ((double)F * F * (double)s2 * s2) : 1.0;
+    int fold_d = -1;
+    uint32_t phase = 0;
+    bool mma_pending = false;
+
+    const long long total = (a.G + a.lag) * (long long)per_block;
+    const int B = a.B;
+    unsigned held = 0;
+    if (tid == 0)
+        held = atomicAdd(a.ticket, 1u);
+    for (unsigned it = 0;; it++)
+    {
+        const int par = it & 1;
+        if (tid == 0)
+        {
+            unsigned t;
+            s_verdict[par] = judge_ticket<n1t, n2t>(a, total, held, t, true);
+            s_ticket[par] = t;
+        }
+        __syncthreads(); // also orders the previous item's shared-memory and TMEM use
+        const int verdict = s_verdict[par];
+        if (verdict < 0)
+            break;
+        if (verdict == 0)
+            continue;
+        const long long t = s_ticket[par];
+        const long long q = t / per_block;
+        const int w = (int)(t % per_block);
+        const bool is_p1 = w < n1t;
+        const long long f = is_p1 ? q : q - a.lag;
+        const int slot = (int)((unsigned)f % (unsigned)a.S);
+        float2 *Ts = a.T + (size_t)slot * F;
+        const long long gi = a.g0 + f;
+        const int d = (int)((unsigned)gi / (unsigned)B), b = (int)((unsigned)gi % (unsigned)B);
+        float2 x[2][16];
+        if (is_p1)
+        {
+            // columns n1 = c0 + v; lanes take consecutive columns (128-byte runs)
+            const int c0 = w * TC_COLS;
+            const int v = lane & 15, bp = 2 * warp + (lane >> 4);
+            const int n0 = c0 + v + N1 * 2 * bp;
+            const float2 *Hd = a.H + (size_t)d * F;
+            const uint16_t *dl = a.delays + (size_t)d * F;
+            const int rb = a.rbi + b;
+            int sl[2][16];
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    sl[i][k] = ld_na(dl + n0 + N1 * (32 * k + i));
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                {
+                    const int n = n0 + N1 * (32 * k + i);
+                    int s = rb - sl[i][k];
+                    if (s < 0)
+                        s += a.fbs;
+                    x[i][k] = cmul(ld_na(a.ring + (size_t)s * F + n), ld_na(Hd + n));
+                }
+            const uint32_t row_off = 128u * v + ((uint32_t)(((bp >> 1) ^ v) & 7) << 4) + 8u * (bp & 1);
+            tc_step1<BF16>(x, W1, bp, row_off, sA_hi, sA_lo);
+        }
+        else
+        {
+            // rows k2 = r0 + v of the row-major slot; lanes take consecutive columns
+            const int r0 = (w - n1t) * TC_COLS;
+            const int bp = lane & 15, v = 2 * warp + (lane >> 4);
+            if constexpr (FOLD)
+            {
+                if (d != fold_d)
+                {
+                    if (fold_d >= 0)
+                        fold_flush(s_bins, a.fold, fold_d, flush_scale2);
+                    fold_d = d;
+                }
+            }
+            const float2 *row = Ts + (size_t)(r0 + v) * N1 + 2 * bp;
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+            {
+                const float4 q4 = __ldcg(reinterpret_cast<const float4 *>(row + 32 * k));
+                x[0][k] = make_float2(q4.x, q4.y);
+                x[1][k] = make_float2(q4.z, q4.w);
+            }
+            const uint32_t row_off = 128u * v + ((uint32_t)(((bp >> 1) ^ v) & 7) << 4) + 8u * (bp & 1);
+            tc_step1<BF16>(x, W2, bp, row_off, sA_hi, sA_lo);
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads(); // A tiles complete; pass 2: every thread holds its slot inputs
+        if (tid == 0)
+        {
+            if (!is_p1) // release: every thread's reads of the slot precede the count
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p2_done + slot) : "memory");
+            tc_issue(tmem, a_hi, a_lo, b_hi + (is_p1 ? 0u : 4096u), b_lo + (is_p1 ? 0u : 4096u),
+                     is_p1 ? IDESC_P1 : IDESC_P2, &mbar);
+        }
+        if (!umma::mbar_wait(&mbar, phase, a.timeout_ns))
+        {
+            atomicExch(a.err, 1); // the next ticket's verdict stops this CTA
+            mma_pending = true;
+        }
+        phase ^= 1u;
+        umma::fence_after_sync();
+        if (is_p1)
+        {
+            // D row (ka, v): X1[n1 = c0 + v][k2 = ka + 16 kb], kb = 0..31, times
+            // W_F^(n1*k2) (and 1/s1) into the row-major slot
+            const int c0 = w * TC_COLS;
+            const int n1 = c0 + acc_v;
+            float c[2][32];
+            umma::tmem_ld32(acc_addr, c[0]);
+            umma::tmem_ld32(acc_addr + 32u, c[1]);
+            float2 tw = twiddle_F(a.tw.lo, a.tw.hi, (unsigned)(n1 * acc_ka), N2 - 1, 9);
+            tw = make_float2(tw.x * inv_s1, tw.y * inv_s1);
+            const float2 step = twiddle_F(a.tw.lo, a.tw.hi, (unsigned)(16 * n1), N2 - 1, 9);
+            float2 *dst = Ts + (size_t)acc_ka * N1 + n1;
+#pragma unroll
+            for (int kb = 0; kb < 32; kb++)
+            {
+                dst[(size_t)kb * 16 * N1] = cmul(make_float2(c[kb >> 4][(2 * kb) & 31], c[kb >> 4][(2 * kb + 1) & 31]), tw);
+                tw = cmul(tw, step);
+            }
+            umma::fence_before_sync();
+            __syncthreads();
+            if (tid == 0)
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p1_done + slot) : "memory");
+        }
+        else
+        {
+            // D row (ka, v): row k2 = r0 + v, outputs k1 = ka + 16 kb for kb = 16..31,
+            // i.e. window samples k2 + N2 * (k1 - 256)
+            const int r0 = (w - n1t) * TC_COLS;
+            float c[32];
+            umma::tmem_ld32(acc_addr, c);
+            umma::fence_before_sync();
+            const size_t rowbase = ((size_t)d * B + b) * M;
+#pragma unroll
+            for (int j = 0; j < 16; j++)
+            {
+                const int k1h = acc_ka + 16 * j;
+                float2 xv = make_float2(c[2 * j], c[2 * j + 1]);
+                if constexpr (MODE != OUT_FOLD)
+                {
+                    xv.x *= out_scale;
+                    xv.y *= out_scale;
+                }
+                const size_t o = rowbase + r0 + acc_v + (size_t)N2 * k1h;
+                if constexpr ((MODE & OUT_C64) != 0)
+                    a.out_c64[o] = xv;
+                if constexpr ((MODE & OUT_U16) != 0)
+                    a.out_u16[o] = encode_u16(xv);
+                if constexpr ((MODE & OUT_POW) != 0)
+                    a.out_pow[o] = xv.x * xv.x + xv.y * xv.y;
+                if constexpr ((MODE & OUT_PAIR) != 0)
+                    s_p[k1h * TC_COLS + acc_v] = sqrtf(__ldcs(a.pair_pow + o) + (xv.x * xv.x + xv.y * xv.y));
+                else if constexpr (FOLD)
+                    s_p[k1h * TC_COLS + acc_v] = xv.x * xv.x + xv.y * xv.y;
+            }
+            if constexpr (FOLD)
+            {
+                __syncthreads();
+                fold_tile<TC_COLS, N1 / 2>(s_p, s_bins,
+                                          a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
+                                          a.fold.dphase, a.fold.K, r0, N2);
+            }
+        }
+    }
+    if constexpr (FOLD)
+    {
+        if (fold_d >= 0)
+            fold_flush(s_bins, a.fold, fold_d, flush_scale2);
+    }
+    // a timed-out item's MMAs may still be running: wait for them once more (bounded)
+    // before the accumulator is released
+    if (mma_pending && tid == 0)
+        (void)umma::mbar_wait(&mbar, phase ^ 1u, a.timeout_ns);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0)
+        umma::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
 // Raise (never lower) this device's persisting-L2 set-aside to `bytes`, capped at the
 // device maximum, once per size.  A failure only costs the hint.
 void ensure_l2_persisting(size_t bytes)
@@ -497,17 +860,13 @@ void ensure_l2_persisting(size_t bytes)
     done[dev] = bytes;
 }
 
-template <int N1, int N2, int MODE>
-cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+// Launch (or, with `plan`, only size) a persistent transform kernel `k` taking
+// (PersistArgs, EXTRA...): grid = resident CTAs per SM (at most max_per_sm) x SMs.
+template <class KERNEL, class... EXTRA>
+cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kMaxDevices], int per_block,
+                                     int max_per_sm, int F, const PersistArgs &a, int sms, cudaStream_t st,
+                                     PersistPlan *plan, EXTRA... extra)
 {
-    using C1 = PCfg<N2>;
-    using C2 = PCfg<N1>;
-    constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
-    auto k = inv_persistent_kernel<N1, N2, MODE>;
-    constexpr bool P1_TWO = LastNs<N2, 1, true>::value == StageRadix<N2, 1, true>::value;
-    const size_t smem = (size_t)(DATA + N1 + (P1_TWO ? N2 : 2 * N2)) * sizeof(float2) +
-                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
-    static size_t granted[kMaxDevices] = {};
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
         return e;
@@ -515,10 +874,10 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P_THREADS, smem);
     if (e != cudaSuccess)
         return e;
+    per_sm = std::min(per_sm, max_per_sm);
     if (per_sm < 1)
         return cudaErrorInvalidConfiguration;
     const int grid = per_sm * sms;
-    constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
     if (plan)
     {
         // Enough look-behind that items in flight rarely wait: every CTA holds its
@@ -537,7 +896,7 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
         return cudaErrorInvalidValue;
     // the pass-1 -> pass-2 slots are re-read within a few items: ask L2 to keep them
     // (persisting window over the slot ring; the streamed spectra and responses miss it)
-    const size_t slot_bytes = (size_t)a.S * (size_t)(N1 * N2) * sizeof(float2);
+    const size_t slot_bytes = (size_t)a.S * (size_t)F * sizeof(float2);
     ensure_l2_persisting(slot_bytes);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -553,8 +912,63 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
     attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, k, a);
+    e = cudaLaunchKernelEx(&cfg, k, a, extra...);
     return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+template <int N1, int N2, int MODE>
+cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    using C1 = PCfg<N2>;
+    using C2 = PCfg<N1>;
+    constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
+    constexpr bool P1_TWO = LastNs<N2, 1, true>::value == StageRadix<N2, 1, true>::value;
+    const size_t smem = (size_t)(DATA + N1 + (P1_TWO ? N2 : 2 * N2)) * sizeof(float2) +
+                        (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
+    static size_t granted[kMaxDevices] = {};
+    constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
+    return launch_persistent_kernel(inv_persistent_kernel<N1, N2, MODE>, smem, granted, per_block, 1 << 20, N1 * N2,
+                                    a, sms, st, plan);
+}
+
+template <int MODE, bool BF16>
+cudaError_t tc_launch(const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    const size_t smem = 1024 + TC_BINS + (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
+    static size_t granted[kMaxDevices] = {};
+    // at most 512 / 128 CTAs per SM can hold their tensor-memory columns at once
+    return launch_persistent_kernel(inv_tc_kernel<MODE, BF16>, smem, granted, 2 * (TC_N / TC_COLS),
+                                    512 / (int)TC_TMEM_COLS, TC_N * TC_N, a, sms, st, plan, tc);
+}
+
+template <bool BF16>
+cudaError_t tc_mode(const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    switch (a.out_mode)
+    {
+    case OUT_C64: return tc_launch<OUT_C64, BF16>(a, tc, sms, st, plan);
+    case OUT_U16: return tc_launch<OUT_U16, BF16>(a, tc, sms, st, plan);
+    case OUT_FOLD: return tc_launch<OUT_FOLD, BF16>(a, tc, sms, st, plan);
+    case OUT_C64 | OUT_FOLD: return tc_launch<OUT_C64 | OUT_FOLD, BF16>(a, tc, sms, st, plan);
+    case OUT_U16 | OUT_FOLD: return tc_launch<OUT_U16 | OUT_FOLD, BF16>(a, tc, sms, st, plan);
+    case OUT_C64 | OUT_U16: return tc_launch<OUT_C64 | OUT_U16, BF16>(a, tc, sms, st, plan);
+    case OUT_POW: return tc_launch<OUT_POW, BF16>(a, tc, sms, st, plan);
+    case OUT_FOLD | OUT_PAIR: return tc_launch<OUT_FOLD | OUT_PAIR, BF16>(a, tc, sms, st, plan);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t tc_dispatch(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st,
+                        PersistPlan *plan)
+{
+    if (L != 18)
+        return cudaErrorInvalidValue;
+    switch (prec)
+    {
+    case PREC_BF16X3: return tc_mode<true>(a, tc, sms, st, plan);
+    case PREC_FP16X3: return tc_mode<false>(a, tc, sms, st, plan);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 template <int N1, int N2>
@@ -645,6 +1059,18 @@ cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan
 cudaError_t launch_inverse_persistent(int L, const PersistArgs &a, int sms, cudaStream_t st)
 {
     return persist_dispatch(L, a, sms, st, nullptr);
+}
+
+bool tc_supported(int L) { return L == 18; }
+
+cudaError_t tc_plan(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, PersistPlan *plan)
+{
+    return tc_dispatch(L, prec, a, tc, sms, nullptr, plan);
+}
+
+cudaError_t launch_inverse_tc(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st)
+{
+    return tc_dispatch(L, prec, a, tc, sms, st, nullptr);
 }
 
 } // namespace msosm

@@ -27,6 +27,21 @@ struct PersistArgs
     unsigned long long timeout_ns;
 };
 
+// Split-precision transform (tensor cores): precisions and extra arguments.
+enum Precision : int
+{
+    PREC_FP32 = 0,   // FP32 register transform (the plain form)
+    PREC_BF16X3 = 1, // DFT contractions on BF16 hi/lo operands, FP32 accumulation
+    PREC_FP16X3 = 2, // the same on FP16 hi/lo operands, power-of-two operand scaling
+};
+
+struct TcArgs
+{
+    const uint4 *bop;       // W_32 operand image: hi (8 KB) then lo (8 KB), K-major 128-byte swizzled
+    const unsigned *absmax; // FP16: running max |component| over the spectra ring (float bits)
+    float hmax;             // FP16: max |H| over the DM trials
+};
+
 struct PersistPlan
 {
     int lag = 0, slots = 0, grid = 0;
@@ -39,5 +54,10 @@ cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned lon
 // Grid and ring geometry for the given sizes / output mode (no launch).
 cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan);
 cudaError_t launch_inverse_persistent(int L, const PersistArgs &a, int sms, cudaStream_t st);
+
+// Split-precision persistent transform (F = 2^18 only).
+bool tc_supported(int L);
+cudaError_t tc_plan(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, PersistPlan *plan);
+cudaError_t launch_inverse_tc(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st);
 
 } // namespace msosm

@@ -26,6 +26,7 @@ HEADER = PKG.parent / "include" / "msosm_gb300.h"
 OK = 0
 IN_U16, IN_C64, IN_I8 = 0, 1, 2
 OUT_NONE, OUT_C64, OUT_U16 = 0, 1, 2
+PREC_FP32, PREC_BF16X3, PREC_FP16X3 = 0, 1, 2
 IN_BYTES = {IN_U16: 4, IN_C64: 8, IN_I8: 2}
 
 _lib = None
@@ -73,6 +74,8 @@ def _declare(L):
     L.msosm_create.argtypes = [F, F, P, I, C.POINTER(P)]
     L.osm_create.argtypes = [F, F, F, C.POINTER(P)]
     L.msosm_init.argtypes = [P, I, I, I, I]
+    L.msosm_set_precision.argtypes = [P, I]
+    L.msosm_get_precision.argtypes = [P]
     L.msosm_get_dims.argtypes = [P, PI, PI, PI, PI, PI, PI, PI]
     L.msosm_get_nd.argtypes = [P, P]
     L.msosm_get_delaycounts.argtypes = [P, P]
@@ -264,6 +267,16 @@ class MsosmGpuBatch:
 
     def load_state(self, buf: np.ndarray, stream=None):
         self._check(lib().msosm_load_state(self._h, buf.ctypes.data, buf.nbytes, _stream(stream)))
+
+    def set_precision(self, precision: int):
+        """PREC_FP32 (default), PREC_BF16X3 or PREC_FP16X3: the inverse transforms' DFT
+        stages on the tensor cores with split 16-bit operands (msosm_set_precision)."""
+        self._check(lib().msosm_set_precision(self._h, int(precision)))
+        return self
+
+    @property
+    def precision(self) -> int:
+        return int(lib().msosm_get_precision(self._h))
 
     def use_response_derivative(self):
         """Outputs become dx/dDM (responses replaced by dH/dDM, delays unchanged)."""

@@ -465,6 +465,7 @@ def run_engine(args, w, rank, world, local):
     del x
 
     proc = eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_C64, eng.OUT_NONE)
+    proc.set_precision(PRECISIONS[args.precision])
     step_n = proc.batch * proc.M
     calls = N // step_n
     fold = eng.FoldGpu(np.float32(w["period"]), bw, step_n, w["nbins"], len(dms))
@@ -553,8 +554,9 @@ def run_engine(args, w, rank, world, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": DTYPES[args.precision], "data": "synthetic",
         "config": {"workload": args.workload, "dm_trials_per_gpu": len(dms), "fft_size": proc.fftpoint,
+                   "precision": args.precision,
                    "M": proc.M, "batch": proc.batch, "samples": N, "phase_bins": w["nbins"],
                    "bandwidth_hz": float(bw), "f0_hz": float(f0), "input": "complex64, 1 pol",
                    "l2": "inputs larger than L2 (512 MB baseband, 1 GB responses, 128 MB spectra ring)",
@@ -570,6 +572,12 @@ def run_engine(args, w, rank, world, local):
     print(json.dumps(line))
 
 
+# inverse-transform arithmetic (msosm_set_precision) and the JSON dtype label of each
+PRECISIONS = {"fp32": 0, "bf16x3": 1, "fp16x3": 2}
+DTYPES = {"fp32": "f32", "bf16x3": "bf16x3 (hi/lo operands, f32 accumulate)",
+          "fp16x3": "f16x3 (hi/lo operands, f32 accumulate)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -583,6 +591,9 @@ def main():
     ap.add_argument("--samples", type=int, default=0, help="override the baseband length (profiling captures)")
     ap.add_argument("--dm-trials", type=int, default=0, help="override the DM-trial count (profiling captures)")
     ap.add_argument("--batch", type=int, default=0, help="override the windows per call")
+    ap.add_argument("--precision", default="fp32", choices=sorted(PRECISIONS),
+                    help="inverse-transform arithmetic: fp32 register DFTs, or tensor-core DFT stages on "
+                         "split bf16/fp16 operands (bf16x3 / fp16x3)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

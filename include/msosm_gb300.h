@@ -83,6 +83,23 @@ int osm_plan(float bw, float dm, float f0, unsigned long *nd_out, unsigned long 
 int msosm_create(float bw, float f0, const float *dms, int num_dms, msosm_t **out);
 int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, int out_mode);
 
+/* ---- split precision ---------------------------------------------------------
+ * No counterpart in the reference (its inverse transforms are cuFFT FP32,
+ * msosm_gpu_batch.cpp:196-199,224-227).  MSOSM_PREC_FP32 (the default) runs the
+ * FP32 register transform.  MSOSM_PREC_BF16X3 / MSOSM_PREC_FP16X3 run the inverse
+ * transforms' 32-point DFT stages as tensor-core (tcgen05) contractions on 16-bit
+ * operands split into hi + lo parts, three products per contraction (hi*hi +
+ * lo*hi + hi*lo) accumulated in FP32; the chirp phase of the responses stays FP64
+ * (msosm_plan_response) and every other step FP32.  FP16 operands are scaled by
+ * powers of two from a running bound on the spectra, so they stay in range.
+ * Available for fftpoint 2^18; MSOSM_ERR_UNSUPPORTED otherwise.  Call after
+ * msosm_init; it may be changed between steps. */
+#define MSOSM_PREC_FP32 0
+#define MSOSM_PREC_BF16X3 1
+#define MSOSM_PREC_FP16X3 2
+int msosm_set_precision(msosm_t *h, int precision);
+int msosm_get_precision(const msosm_t *h);
+
 /* Planning results: M, M_min, F = 2M, batch, DM count, processor-wide delaycount
  * and the number of spectra kept in the ring (fft_block_size).  Any pointer may
  * be NULL.  Replaces the public members M, M_min, numDMs, delaycount of
