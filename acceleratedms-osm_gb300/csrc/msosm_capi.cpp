@@ -261,6 +261,7 @@ struct msosm_s
     // split-precision transform (tensor cores): precision, W_32 operand image, FP16
     // operand-scale bound (running max |component| of the ring) and max |H|
     int precision = msosm::PREC_FP32;
+    msosm::PersistPlan last_plan{}; // geometry of the last persistent launch
     void *d_tc_op = nullptr;
     unsigned *d_absmax = nullptr;
     float hmax = 1.0f;
@@ -655,6 +656,8 @@ extern "C" int msosm_set_precision(msosm_t *h, int precision)
     }
     if (!h->persist || !msosm::tc_supported(h->g.L))
         return h->fail(MSOSM_ERR_UNSUPPORTED, "the split-precision transform is built for fftpoint 2^18 only");
+    if ((unsigned long long)h->fbs * (unsigned long long)h->F >= (1ull << 32))
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "spectra ring too long for the split-precision transform");
     cudaError_t e;
     if (!h->d_tc_op && (e = cudaMalloc(&h->d_tc_op, 16384)) != cudaSuccess)
         return h->cuda_fail(e, "cudaMalloc(tensor-core operand)");
@@ -673,6 +676,21 @@ extern "C" int msosm_set_precision(msosm_t *h, int precision)
 extern "C" int msosm_get_precision(const msosm_t *h)
 {
     return h ? h->precision : -1;
+}
+
+extern "C" int msosm_get_launch_info(const msosm_t *h, int *grid, int *occupancy, int *lag, int *slots)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (grid)
+        *grid = h->last_plan.grid;
+    if (occupancy)
+        *occupancy = h->last_plan.occupancy;
+    if (lag)
+        *lag = h->last_plan.lag;
+    if (slots)
+        *slots = h->last_plan.slots;
+    return MSOSM_OK;
 }
 
 extern "C" int msosm_get_dims(const msosm_t *h, int *M, int *M_min, int *fftpoint, int *batch, int *num_dms,
@@ -852,6 +870,8 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
             return h->cuda_fail(e, "persistent transform plan");
         pa.lag = plan.lag;
         pa.S = std::min(plan.slots, h->T_slots);
+        h->last_plan = plan;
+        h->last_plan.slots = pa.S;
         if (pa.S <= pa.lag)
             return h->fail(MSOSM_ERR_UNSUPPORTED, "intermediate ring too small for the persistent transform");
         if ((e = cudaMemsetAsync(h->d_sync, 0, sizeof(unsigned) * (1 + 2 * kMaxSlots), st)) != cudaSuccess)

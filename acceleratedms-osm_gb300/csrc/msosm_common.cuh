@@ -1,5 +1,6 @@
 // Shared device helpers of the MS-OSM kernels.
 #pragma once
+#include <algorithm>
 #include "fft_tile.cuh"
 #include "msosm_kernels.cuh"
 
@@ -123,6 +124,28 @@ inline cudaError_t ensure_smem(KERNEL k, size_t bytes, size_t (&granted)[kMaxDev
     if (e == cudaSuccess)
         granted[dev] = bytes;
     return e;
+}
+
+// Prefer a shared-memory carveout that holds `blocks` CTAs of `dyn_bytes` dynamic
+// shared memory each (plus static and per-CTA reserved bytes), rounded down to a
+// whole percent: the driver rounds a carveout up to the next configuration it has.
+template <class KERNEL>
+inline cudaError_t prefer_carveout(KERNEL k, size_t dyn_bytes, int blocks)
+{
+    int dev = 0, per_sm = 0, reserved = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+        return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k)) != cudaSuccess)
+        return e;
+    if (per_sm <= 0)
+        return cudaSuccess;
+    const size_t need = (size_t)blocks * (dyn_bytes + fa.sharedSizeBytes + (size_t)reserved);
+    const int pct = (int)std::min<size_t>(100, need * 100 / (size_t)per_sm);
+    return cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
 }
 
 } // namespace msosm

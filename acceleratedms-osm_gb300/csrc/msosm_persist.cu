@@ -564,8 +564,9 @@ __device__ __forceinline__ void tc_step1(float2 (&x)[2][16], const float2 *__res
     }
 }
 
-// Thread 0: the 24 MMAs of one item (two A tiles x three products x four K-steps),
-// then a commit that completes the mbarrier's phase when they are done.
+// Thread 0: the 24 MMAs of one item (two A tiles x three products x four K-steps).
+// Each tile's 12 MMAs end with a commit to that tile's mbarrier, so the warps that
+// read tile 0's accumulator start while tile 1's MMAs still run.
 __device__ __forceinline__ void tc_issue(uint32_t tmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
                                          uint32_t idesc, uint64_t *mbar)
 {
@@ -584,8 +585,8 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem, uint32_t a_hi, uint32_t 
 #pragma unroll
         for (int ks = 0; ks < 4; ks++)
             umma::mma_f16(d, umma::desc_sw128(ah + 32u * ks), umma::desc_sw128(b_lo + 32u * ks), idesc, 1u);
+        umma::commit(mbar + t);
     }
-    umma::commit(mbar);
 }
 
 template <int MODE, bool BF16>
@@ -597,7 +598,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
     constexpr uint32_t IDESC_P1 = umma::idesc_f16(128, 64, BF16);
     constexpr uint32_t IDESC_P2 = umma::idesc_f16(128, 32, BF16);
     extern __shared__ unsigned char smem_raw[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[2]; // MMAs of accumulator tile 0 / tile 1 done
     __shared__ uint32_t tmem_slot;
     __shared__ unsigned s_ticket[2];
     __shared__ int s_verdict[2];
@@ -640,7 +641,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
     if (warp == 0)
         umma::tmem_alloc(&tmem_slot, TC_TMEM_COLS);
     if (tid == 0)
-        umma::mbar_init(&mbar, 1);
+    {
+        umma::mbar_init(&mbar[0], 1);
+        umma::mbar_init(&mbar[1], 1);
+    }
     umma::fence_async_smem();
     umma::fence_before_sync();
     __syncthreads();
@@ -713,7 +717,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
                     int s = rb - sl[i][k];
                     if (s < 0)
                         s += a.fbs;
-                    x[i][k] = cmul(ld_na(a.ring + (size_t)s * F + n), ld_na(Hd + n));
+                    // 32-bit element offset: fbs * F < 2^32 (host check)
+                    x[i][k] = cmul(ld_na(a.ring + ((unsigned)s * (unsigned)F + (unsigned)n)), ld_na(Hd + n));
                 }
             const uint32_t row_off = 128u * v + ((uint32_t)(((bp >> 1) ^ v) & 7) << 4) + 8u * (bp & 1);
             tc_step1<BF16>(x, W1, bp, row_off, sA_hi, sA_lo);
@@ -751,9 +756,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
             if (!is_p1) // release: every thread's reads of the slot precede the count
                 asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p2_done + slot) : "memory");
             tc_issue(tmem, a_hi, a_lo, b_hi + (is_p1 ? 0u : 4096u), b_lo + (is_p1 ? 0u : 4096u),
-                     is_p1 ? IDESC_P1 : IDESC_P2, &mbar);
+                     is_p1 ? IDESC_P1 : IDESC_P2, mbar);
         }
-        if (!umma::mbar_wait(&mbar, phase, a.timeout_ns))
+        // this warp's accumulator tile (and, for tile 1, every MMA of the item) is done
+        if (!umma::mbar_wait(&mbar[acc_t], phase, a.timeout_ns))
         {
             atomicExch(a.err, 1); // the next ticket's verdict stops this CTA
             mma_pending = true;
@@ -832,7 +838,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
     // a timed-out item's MMAs may still be running: wait for them once more (bounded)
     // before the accumulator is released
     if (mma_pending && tid == 0)
-        (void)umma::mbar_wait(&mbar, phase ^ 1u, a.timeout_ns);
+        (void)umma::mbar_wait(&mbar[1], phase ^ 1u, a.timeout_ns);
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0)
@@ -862,19 +868,27 @@ void ensure_l2_persisting(size_t bytes)
 
 // Launch (or, with `plan`, only size) a persistent transform kernel `k` taking
 // (PersistArgs, EXTRA...): grid = resident CTAs per SM (at most max_per_sm) x SMs.
+// carveout_blocks > 0: ask for a shared-memory carveout that holds that many CTAs
+// (the occupancy query and the launch otherwise assume a smaller default split).
 template <class KERNEL, class... EXTRA>
 cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kMaxDevices], int per_block,
-                                     int max_per_sm, int F, const PersistArgs &a, int sms, cudaStream_t st,
-                                     PersistPlan *plan, EXTRA... extra)
+                                     int max_per_sm, int carveout_blocks, int F, const PersistArgs &a, int sms,
+                                     cudaStream_t st, PersistPlan *plan, EXTRA... extra)
 {
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
+        return e;
+    if (carveout_blocks > 0 && (e = prefer_carveout(k, smem, carveout_blocks)) != cudaSuccess)
         return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P_THREADS, smem);
     if (e != cudaSuccess)
         return e;
-    per_sm = std::min(per_sm, max_per_sm);
+    const int occupancy = per_sm;
+    // the occupancy query does not see the carveout preference: a kernel that asked
+    // for room for carveout_blocks CTAs is launched with that many per SM (the
+    // ticket order is deadlock-free whatever the residency)
+    per_sm = std::min(std::max(per_sm, carveout_blocks), max_per_sm);
     if (per_sm < 1)
         return cudaErrorInvalidConfiguration;
     const int grid = per_sm * sms;
@@ -888,6 +902,7 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
         plan->lag = (2 * grid + per_block - 1) / per_block + 1;
         plan->slots = 2 * plan->lag;
         plan->grid = grid;
+        plan->occupancy = occupancy;
         return cudaSuccess;
     }
     // the kernel indexes transforms and tickets in 32 bits
@@ -927,8 +942,8 @@ cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, Persi
                         (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
     static size_t granted[kMaxDevices] = {};
     constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
-    return launch_persistent_kernel(inv_persistent_kernel<N1, N2, MODE>, smem, granted, per_block, 1 << 20, N1 * N2,
-                                    a, sms, st, plan);
+    return launch_persistent_kernel(inv_persistent_kernel<N1, N2, MODE>, smem, granted, per_block, 1 << 20, 0,
+                                    N1 * N2, a, sms, st, plan);
 }
 
 template <int MODE, bool BF16>
@@ -938,7 +953,7 @@ cudaError_t tc_launch(const PersistArgs &a, const TcArgs &tc, int sms, cudaStrea
     static size_t granted[kMaxDevices] = {};
     // at most 512 / 128 CTAs per SM can hold their tensor-memory columns at once
     return launch_persistent_kernel(inv_tc_kernel<MODE, BF16>, smem, granted, 2 * (TC_N / TC_COLS),
-                                    512 / (int)TC_TMEM_COLS, TC_N * TC_N, a, sms, st, plan, tc);
+                                    512 / (int)TC_TMEM_COLS, 2, TC_N * TC_N, a, sms, st, plan, tc);
 }
 
 template <bool BF16>
@@ -961,7 +976,8 @@ cudaError_t tc_mode(const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_
 cudaError_t tc_dispatch(int L, int prec, const PersistArgs &a, const TcArgs &tc, int sms, cudaStream_t st,
                         PersistPlan *plan)
 {
-    if (L != 18)
+    // spectra-ring element offsets are 32-bit in the kernel
+    if (L != 18 || (unsigned long long)a.fbs * (1ull << L) >= (1ull << 32))
         return cudaErrorInvalidValue;
     switch (prec)
     {

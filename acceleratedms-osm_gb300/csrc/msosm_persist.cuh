@@ -45,6 +45,7 @@ struct TcArgs
 struct PersistPlan
 {
     int lag = 0, slots = 0, grid = 0;
+    int occupancy = 0; // CTAs per SM the occupancy query reported
 };
 
 bool persist_supported(int L);

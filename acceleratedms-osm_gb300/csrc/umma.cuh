@@ -96,14 +96,15 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity)
+// Suspends the thread until the phase completes or about suspend_ns pass.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity, uint32_t suspend_ns = 20000)
 {
     uint32_t ok;
     asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(ok)
-                 : "r"(smem_addr(mbar)), "r"(parity)
+                 : "r"(smem_addr(mbar)), "r"(parity), "r"(suspend_ns)
                  : "memory");
     return ok != 0;
 }

@@ -75,6 +75,7 @@ def _declare(L):
     L.osm_create.argtypes = [F, F, F, C.POINTER(P)]
     L.msosm_init.argtypes = [P, I, I, I, I]
     L.msosm_set_precision.argtypes = [P, I]
+    L.msosm_get_launch_info.argtypes = [P, PI, PI, PI, PI]
     L.msosm_get_precision.argtypes = [P]
     L.msosm_get_dims.argtypes = [P, PI, PI, PI, PI, PI, PI, PI]
     L.msosm_get_nd.argtypes = [P, P]
@@ -273,6 +274,12 @@ class MsosmGpuBatch:
         stages on the tensor cores with split 16-bit operands (msosm_set_precision)."""
         self._check(lib().msosm_set_precision(self._h, int(precision)))
         return self
+
+    def launch_info(self) -> dict:
+        """Geometry of the last persistent inverse-transform launch."""
+        v = [C.c_int() for _ in range(4)]
+        self._check(lib().msosm_get_launch_info(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("grid", "occupancy", "lag", "slots"), (x.value for x in v)))
 
     @property
     def precision(self) -> int:

@@ -556,7 +556,7 @@ def run_engine(args, w, rank, world, local):
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPES[args.precision], "data": "synthetic",
         "config": {"workload": args.workload, "dm_trials_per_gpu": len(dms), "fft_size": proc.fftpoint,
-                   "precision": args.precision,
+                   "precision": args.precision, "persistent_launch": proc.launch_info(),
                    "M": proc.M, "batch": proc.batch, "samples": N, "phase_bins": w["nbins"],
                    "bandwidth_hz": float(bw), "f0_hz": float(f0), "input": "complex64, 1 pol",
                    "l2": "inputs larger than L2 (512 MB baseband, 1 GB responses, 128 MB spectra ring)",

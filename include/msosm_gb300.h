@@ -100,6 +100,11 @@ int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, int out_mode)
 int msosm_set_precision(msosm_t *h, int precision);
 int msosm_get_precision(const msosm_t *h);
 
+/* Geometry of the handle's last persistent inverse-transform launch (F >= 2^16):
+ * CTAs, CTAs per SM the occupancy query reported, look-behind and intermediate
+ * slots; zeros before the first such launch.  No counterpart in the reference. */
+int msosm_get_launch_info(const msosm_t *h, int *grid, int *occupancy, int *lag, int *slots);
+
 /* Planning results: M, M_min, F = 2M, batch, DM count, processor-wide delaycount
  * and the number of spectra kept in the ring (fft_block_size).  Any pointer may
  * be NULL.  Replaces the public members M, M_min, numDMs, delaycount of
