@@ -23,7 +23,8 @@ LIB = LIB_DIR / "libmsosm_gb300.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["msosm_forward.cu", "msosm_inverse.cu", "msosm_persist.cu", "msosm_fold.cu", "msosm_noalloc.cu", "msosm_tc.cu"]
+CU_SOURCES = ["msosm_forward.cu", "msosm_inverse.cu", "msosm_persist.cu", "msosm_fold.cu", "msosm_noalloc.cu", "msosm_tc.cu",
+              "msosm_sim.cu"]
 CPP_SOURCES = ["msosm_plan.cpp", "msosm_capi.cpp", "msosm_writer.cpp"]
 
 

@@ -14,6 +14,7 @@
 // The work is ordered on the caller's stream (the copy stream joins it through
 // events); nothing synchronises the device.
 #include "msosm_gb300.h"
+#include "msosm_internal.h"
 
 #include "msosm_kernels.cuh"
 #include "msosm_persist.cuh"
@@ -444,6 +445,27 @@ extern "C" int osm_create(float bw, float dm, float f0, msosm_t **out)
     h->nd.assign(1, (int)nd);
     const unsigned long mmin = msosm::plan_osm_min_order(nd);
     h->M_min = (int)std::min<unsigned long>(mmin, 1ul << 30);
+    *out = h;
+    return MSOSM_OK;
+}
+
+int msosm_filter_create(float bw, float f0, int M, msosm_t **out)
+{
+    if (!out)
+        return MSOSM_ERR_ARG;
+    *out = nullptr;
+    if (!(bw > 0) || !(f0 > 0) || M < 1 || !is_pow2(M))
+        return MSOSM_ERR_ARG;
+    msosm_t *h = new (std::nothrow) msosm_s();
+    if (!h)
+        return MSOSM_ERR_NOMEM;
+    h->osm = true;
+    h->bw = bw;
+    h->f0 = f0;
+    h->dms.assign(1, 0.0f);
+    h->D = 1;
+    h->nd.assign(1, 0);
+    h->M_min = M;
     *out = h;
     return MSOSM_OK;
 }
@@ -929,6 +951,20 @@ extern "C" int msosm_attach_writer(msosm_t *h, msosm_writer_t *w)
     return MSOSM_OK;
 }
 
+extern "C" int msosm_writer_copy_output(msosm_writer_t *w, msosm_t *h, void *stream)
+{
+    if (!h || !w)
+        return MSOSM_ERR_ARG;
+    if (!h->inited || !h->d_out_u16)
+        return h->fail(MSOSM_ERR_STATE, "writer_copy_output needs an initialised handle with MSOSM_OUT_U16");
+    if (msosm::writer_num_files(w) != h->D ||
+        msosm::writer_bytes_per_step(w) != (size_t)h->D * h->B * h->M * sizeof(uint32_t))
+        return h->fail(MSOSM_ERR_ARG, "writer must have one file per DM and B*M*4 bytes per DM per step");
+    std::string werr;
+    const int rc = msosm::writer_submit_device(w, h->d_out_u16, (cudaStream_t)stream, werr);
+    return rc == MSOSM_OK ? rc : h->fail(rc, werr);
+}
+
 extern "C" int msosm_process(msosm_t *h, const void *in, void *stream)
 {
     return msosm_process_many(h, in, 1, stream);
@@ -1153,6 +1189,25 @@ extern "C" int msosm_plan_response_derivative(float bw, float f0, float dm, int 
         return MSOSM_ERR_ARG;
     msosm::plan_responses(bw, f0, &dm, 1, M, H_out, 1, true);
     return MSOSM_OK;
+}
+
+extern "C" int msosm_set_response(msosm_t *h, int dm_index, const float *H)
+{
+    if (!h || !H)
+        return MSOSM_ERR_ARG;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "set_response before init");
+    if (dm_index < 0 || dm_index >= h->D)
+        return h->fail(MSOSM_ERR_ARG, "dm_index out of range");
+    const bool dev = is_device_pointer(H);
+    std::vector<float> host(2 * (size_t)h->F);
+    cudaError_t e = cudaMemcpy(host.data(), H, host.size() * sizeof(float), dev ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
+    if (e != cudaSuccess)
+        return h->cuda_fail(e, "cudaMemcpy(H)");
+    // the FP16 operand scaling needs a bound on |H| over every row
+    h->hmax = std::max(h->hmax, max_abs_complex(host));
+    e = cudaMemcpy(h->d_H + (size_t)dm_index * h->F, host.data(), (size_t)h->F * sizeof(float2), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? MSOSM_OK : h->cuda_fail(e, "cudaMemcpy(H)");
 }
 
 extern "C" int msosm_use_response_derivative(msosm_t *h)

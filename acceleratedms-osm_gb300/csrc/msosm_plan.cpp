@@ -231,4 +231,43 @@ void plan_responses(float bw, float f0, const float *dms, int n, int M, float *H
         th.join();
 }
 
+void plan_dispersion_response(float bw, float f0, float dm, unsigned long nd, int F, float *Hout)
+{
+    const double kdm_d = 4.15e15;
+    const double fs_d = (double)bw, dm_d = (double)dm, f0_d = (double)f0;
+    const double w0_d = 2.0 * kPi * f0_d;
+    size_t fp = 1;
+    while (fp < nd + 1)
+        fp <<= 1;
+    // chirp at fp bins: bin k < fp/2 sits fs/2 + k*fs/fp above the band's lower edge,
+    // bin k >= fp/2 at k*fs/fp - fs/2
+    std::vector<cd> h(fp);
+    const double step = fs_d / (double)fp;
+    for (size_t k = 0; k < fp; k++)
+    {
+        const double f = (k < fp / 2) ? fs_d / 2.0 + (double)k * step : (double)k * step - fs_d / 2.0;
+        const double w = 2.0 * kPi * f;
+        const double phase = 4.0 * kPi * kPi * kdm_d * dm_d * w * w / ((w + w0_d) * w0_d * w0_d);
+        h[k] = cd(std::cos(phase), std::sin(phase));
+    }
+    if (fp > 1)
+    {
+        const std::vector<cd> tw = make_table((int)fp);
+        fft_inplace(h.data(), (int)fp, +1, tw.data());
+    }
+    const double inv = 1.0 / (double)fp;
+    // the response occupies indices fp-nd .. fp-1 and 0 (negative times): make it causal
+    std::vector<cd> H((size_t)F, cd(0.0, 0.0));
+    for (unsigned long j = 0; j < nd; j++)
+        H[j] = h[fp - nd + j] * inv;
+    H[nd] = h[0] * inv;
+    const std::vector<cd> twF = make_table(F);
+    fft_inplace(H.data(), F, -1, twF.data());
+    for (int k = 0; k < F; k++)
+    {
+        Hout[2 * (size_t)k] = (float)H[k].real();
+        Hout[2 * (size_t)k + 1] = (float)H[k].imag();
+    }
+}
+
 } // namespace msosm

@@ -31,4 +31,12 @@ void plan_response(float bw, float f0, float dm, int M, float *Hout);
 void plan_responses(float bw, float f0, const float *dms, int n, int M, float *Hout, int threads,
                     bool derivative = false);
 
+// Causal dispersion response for the simulator: the chirp exp(+i phi) sampled at
+// fp = next_pow2(nd + 1) bins with the generator's frequency mapping
+// (simulated_complex_signal.cpp:347-366), its inverse transform / fp, the
+// nd + 1 taps of the physical (negative-time) response moved to indices 0..nd
+// (:374-385), zero-padded to F and transformed (:387-389); FP64 throughout,
+// rounded to complex64 once.  Hout: F interleaved (re, im) floats; F >= 2 (nd + 1).
+void plan_dispersion_response(float bw, float f0, float dm, unsigned long nd, int F, float *Hout);
+
 } // namespace msosm

@@ -10,6 +10,7 @@ Class names follow the reference's processors:
   MsosmGpuBatch  ~ MSOSM_GPU_BATCH (dedispersion/include/msosm_gpu_batch.h:13-97)
   OsmGpuBatch    ~ OSM_GPU_BATCH   (dedispersion/include/osm_gpu_batch.h:7-38)
   FoldGpu        ~ Fold_GPU        (folding/include/fold_gpu.h:10-43)
+  Simulator      ~ SimulatedComplexSignal + AWGN (simulated_pulsar/include/*.h)
 """
 from __future__ import annotations
 
@@ -130,6 +131,21 @@ def _declare(L):
     L.msosm_plan_segmentation.argtypes = [F, F, F, I, I, P, P]
     L.msosm_plan_response.argtypes = [F, F, F, I, P]
     L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
+    L.msosm_set_response.argtypes = [P, I, P]
+    L.msosm_writer_copy_output.argtypes = [P, P, P]
+    ULL = C.c_ulonglong
+    L.msosm_sim_create.argtypes = [F, F, F, F, C.POINTER(P)]
+    L.msosm_sim_set_pulse.argtypes = [P, I, F]
+    L.msosm_sim_set_noise.argtypes = [P, I, F]
+    L.msosm_sim_set_seed.argtypes = [P, ULL]
+    L.msosm_sim_info.argtypes = [P, C.POINTER(ULL), C.POINTER(ULL), C.POINTER(D), C.POINTER(D)]
+    L.msosm_sim_generate.argtypes = [P, ULL, I, F, P, P]
+    L.msosm_sim_position.restype = ULL
+    L.msosm_sim_position.argtypes = [P]
+    L.msosm_sim_last_error.restype = C.c_char_p
+    L.msosm_sim_last_error.argtypes = [P]
+    L.msosm_sim_destroy.argtypes = [P]
+    L.msosm_awgn.argtypes = [ULL, ULL, ULL, F, F, P, P]
 
 
 def plan_nd(bw, f0, dms) -> np.ndarray:
@@ -352,6 +368,60 @@ class OsmGpuBatch(MsosmGpuBatch):
 
     def __init__(self, bw: float, dm: float, f0: float):
         super().__init__(bw, None, f0, _osm_dm=dm)
+
+
+SIM_TEST_PULSE, SIM_GAUSSIAN, SIM_IMPULSES = 0, 1, 2
+
+
+class Simulator:
+    """Dispersed-pulsar baseband generated on the GPU (msosm_sim_*): the
+    simulated_pulsar front end with a counter-based seeded generator."""
+
+    def __init__(self, bw: float, f0: float, dm: float, period: float, *, kind: int = SIM_TEST_PULSE,
+                 duty: float = 0.05, snr_db: float | None = None, seed: int = 1):
+        L = lib()
+        self._h = P()
+        rc = L.msosm_sim_create(bw, f0, dm, period, C.byref(self._h))
+        if rc != OK:
+            raise MsosmError(f"msosm_sim_create: {L.msosm_status_string(rc).decode()}")
+        self._check(L.msosm_sim_set_pulse(self._h, kind, duty))
+        self._check(L.msosm_sim_set_noise(self._h, int(snr_db is not None), float(snr_db or 0.0)))
+        self._check(L.msosm_sim_set_seed(self._h, int(seed)))
+        np_, nd = C.c_ulonglong(), C.c_ulonglong()
+        ps, ns = C.c_double(), C.c_double()
+        self._check(L.msosm_sim_info(self._h, C.byref(np_), C.byref(nd), C.byref(ps), C.byref(ns)))
+        self.period_samples, self.nd = np_.value, nd.value
+        self.signal_power, self.noise_sigma = ps.value, ns.value
+
+    def _check(self, rc):
+        if rc != OK:
+            raise MsosmError(f"{lib().msosm_status_string(rc).decode()}: {lib().msosm_sim_last_error(self._h).decode()}")
+
+    def generate(self, n: int, fmt: int = IN_C64, scale: float = 1.0, out=None, stream=None):
+        """The next n samples, into `out` (host array or device tensor) or a new numpy array."""
+        if out is None:
+            dt = {IN_C64: np.complex64, IN_U16: np.uint32, IN_I8: np.int8}[fmt]
+            out = np.zeros(n * (2 if fmt == IN_I8 else 1), dt)
+        self._check(lib().msosm_sim_generate(self._h, int(n), fmt, float(scale), _ptr(out), _stream(stream)))
+        return out
+
+    @property
+    def position(self) -> int:
+        return int(lib().msosm_sim_position(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.msosm_sim_destroy(self._h)
+            self._h = None
+
+
+def awgn(n: int, mean: float = 0.0, stddev: float = 1.0, seed: int = 1, first: int = 0, out=None, stream=None):
+    """n complex samples with independent N(mean, stddev^2) quadratures (msosm_awgn)."""
+    if out is None:
+        out = np.zeros(n, np.complex64)
+    if lib().msosm_awgn(int(seed), int(first), int(n), float(mean), float(stddev), _ptr(out), _stream(stream)) != OK:
+        raise MsosmError("msosm_awgn")
+    return out
 
 
 class FoldGpu:

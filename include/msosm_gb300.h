@@ -214,6 +214,10 @@ typedef struct msosm_writer_s msosm_writer_t;
 int msosm_writer_create(const char *dir, const char *prefix, const float *dms, int num_dms,
                         unsigned long long bytes_per_dm, int slots, int direct_io, msosm_writer_t **out);
 int msosm_attach_writer(msosm_t *h, msosm_writer_t *w);
+/* copy_to_slot (msosm_data_save_uring.cpp:100-110) for a handle without an attached
+ * writer: the handle's last uint16 output into a free slot on `stream`, then written
+ * by a worker at the next step offset; blocks while every slot is busy. */
+int msosm_writer_copy_output(msosm_writer_t *w, msosm_t *h, void *stream);
 int msosm_writer_write(msosm_writer_t *w, const void *host_block);
 int msosm_writer_join(msosm_writer_t *w);
 const char *msosm_writer_last_error(const msosm_writer_t *w);
@@ -293,6 +297,55 @@ int msosm_attach_fold(msosm_t *h, msosm_fold_t *f);
  * Both handles: same DMs, batch and fftpoint (>= 65536), MSOSM_OUT_NONE. f = NULL
  * detaches both. */
 int msosm_attach_fold_pol2(msosm_t *first, msosm_t *second, msosm_fold_t *f);
+
+/* Replace DM trial dm_index's response by a caller-supplied one: F complex64 bins
+ * (2F interleaved floats, host or device) in the transform's natural bin order.
+ * No counterpart in the reference (its responses come only from
+ * generate_dedisp_params, msosm_prepare.cpp:107-164). */
+int msosm_set_response(msosm_t *h, int dm_index, const float *H);
+
+/* ---- simulated pulsar baseband ---------------------------------------------------
+ * Replaces SimulatedComplexSignal (simulated_pulsar/include/simulated_complex_signal.h:7-55,
+ * simulated_complex_signal.cpp) and AWGN (simulated_pulsar/include/AWGN.h:8-17,
+ * AWGN.cpp:3-58), generated on the GPU:
+ * msosm_sim_create     SimulatedComplexSignal(bw, dm, f0, period): Np = period*fs
+ *                      samples per period, Nd as Prepare_OSM computes it (:16-30)
+ * msosm_sim_set_pulse  MSOSM_SIM_TEST_PULSE: the generator's three-component test
+ *                      profile times complex Gaussian noise, a new realisation every
+ *                      period (generate_test_pulse, :44-72); MSOSM_SIM_GAUSSIAN: one
+ *                      Gaussian component of FWHM duty*period at phase 0.5;
+ *                      MSOSM_SIM_IMPULSES: two impulses of 32767 per period at Np/2
+ *                      and Np/2 + 2 (generate_pulsar_signal, :563-571)
+ * msosm_sim_set_noise  additive complex AWGN at per-sample SNR snr_db against the
+ *                      emission's mean power (generate_pulsar_signal's add_noise, SNR)
+ * msosm_sim_generate   the next n samples of the dispersed stream (causal dispersion
+ *                      response applied by the engine's overlap-save transform, its
+ *                      Nd-sample delay skipped, :347-442), times `scale`, encoded as
+ *                      MSOSM_IN_C64 / MSOSM_IN_U16 (offset binary, 0 kept as "no data")
+ *                      / MSOSM_IN_I8 into `out` (host: returns with the data there;
+ *                      device: asynchronous on `stream`).  Consecutive calls continue
+ *                      the stream; every sample depends only on the seed and its index.
+ * msosm_sim_info       Np, Nd, mean emission power per sample, noise sigma per quadrature
+ * msosm_awgn           AWGN::generateNoiseSamples: n complex samples (2n floats, host or
+ *                      device) with independent N(mean, stddev^2) quadratures, samples
+ *                      first .. first+n-1 of the seed's noise stream.
+ * Dispersion smear is limited to Nd < 2^21 samples (filter transform <= 2^22 points). */
+#define MSOSM_SIM_TEST_PULSE 0
+#define MSOSM_SIM_GAUSSIAN 1
+#define MSOSM_SIM_IMPULSES 2
+typedef struct msosm_sim_s msosm_sim_t;
+int msosm_sim_create(float bw, float f0, float dm, float period, msosm_sim_t **out);
+int msosm_sim_set_pulse(msosm_sim_t *s, int kind, float duty);
+int msosm_sim_set_noise(msosm_sim_t *s, int enable, float snr_db);
+int msosm_sim_set_seed(msosm_sim_t *s, unsigned long long seed);
+int msosm_sim_info(const msosm_sim_t *s, unsigned long long *period_samples, unsigned long long *nd,
+                   double *signal_power, double *noise_sigma);
+int msosm_sim_generate(msosm_sim_t *s, unsigned long long n, int out_format, float scale, void *out, void *stream);
+unsigned long long msosm_sim_position(const msosm_sim_t *s);
+const char *msosm_sim_last_error(const msosm_sim_t *s);
+int msosm_sim_destroy(msosm_sim_t *s);
+int msosm_awgn(unsigned long long seed, unsigned long long first, unsigned long long n, float mean, float stddev,
+               float *out, void *stream);
 
 /* ---- overlap-save filtering without device allocation --------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate
