@@ -22,6 +22,8 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../msosm_gb300.h"
 
 using namespace std;
@@ -91,6 +93,19 @@ inline void plot(vector<double> &v) { msosm_compat::dump_series(v.size(), [&](si
 
 // CUDA_CHECK-style failure: print and exit(1), as the reference's processors do
 // (gpu/include/gpu_common.cuh:42-62).  The C ABI itself only returns codes.
+#ifndef CUDA_CHECK
+#define CUDA_CHECK(call)                                                                                    \
+    do                                                                                                      \
+    {                                                                                                       \
+        const cudaError_t msosm_compat_e = (call);                                                          \
+        if (msosm_compat_e != cudaSuccess)                                                                  \
+        {                                                                                                   \
+            cerr << "CUDA error: " << cudaGetErrorString(msosm_compat_e) << " at " << __FILE__ << ":"       \
+                 << __LINE__ << endl;                                                                       \
+            exit(1);                                                                                        \
+        }                                                                                                   \
+    } while (0)
+#endif
 namespace msosm_compat {
 inline void check(int rc, msosm_t *h, const char *what)
 {

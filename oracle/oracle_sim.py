@@ -25,15 +25,10 @@ _M0, _M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
 _W0, _W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
 
 
-def philox4x32_10(idx: np.ndarray, stream: int, seed: int):
-    """Four 32-bit words per counter value idx (uint64 array)."""
-    idx = idx.astype(np.uint64)
-    c0 = idx & _MASK
-    c1 = idx >> np.uint64(32)
-    c2 = np.full_like(c0, np.uint64(stream))
-    c3 = np.zeros_like(c0)
-    k0 = np.uint64(seed & 0xFFFFFFFF)
-    k1 = np.uint64((seed >> 32) & 0xFFFFFFFF)
+def philox_rounds(c0, c1, c2, c3, k0: int, k1: int):
+    """Philox-4x32-10 of counter words c0..c3 (uint64 arrays of 32-bit values), key (k0, k1)."""
+    c0, c1, c2, c3 = (np.asarray(c, np.uint64) for c in (c0, c1, c2, c3))
+    k0, k1 = np.uint64(k0), np.uint64(k1)
     for _ in range(10):
         p0 = _M0 * c0
         p1 = _M1 * c2
@@ -41,6 +36,15 @@ def philox4x32_10(idx: np.ndarray, stream: int, seed: int):
         k0 = (k0 + _W0) & _MASK
         k1 = (k1 + _W1) & _MASK
     return c0, c1, c2, c3
+
+
+def philox4x32_10(idx: np.ndarray, stream: int, seed: int):
+    """Four 32-bit words per sample index idx: counter (idx_lo, idx_hi, stream, 0),
+    key (seed_lo, seed_hi)."""
+    idx = idx.astype(np.uint64)
+    c0 = idx & _MASK
+    return philox_rounds(c0, idx >> np.uint64(32), np.full_like(c0, np.uint64(stream)), np.zeros_like(c0),
+                         seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
 
 
 def normal_pairs(idx: np.ndarray, stream: int, seed: int) -> np.ndarray:

@@ -6,6 +6,8 @@ exports); `-m gpu` needs a CUDA device and calls the engine through the C ABI.
 from __future__ import annotations
 
 import json
+import os
+import shutil
 import sys
 from pathlib import Path
 
@@ -16,6 +18,18 @@ ROOT = Path(__file__).resolve().parents[1]
 GOLDEN = ROOT / "tests" / "golden"
 sys.path.insert(0, str(ROOT / "oracle"))
 sys.path.insert(0, str(ROOT / "acceleratedms-osm_gb300"))
+
+
+# The reference source tree, for the tests that compile its programs against the
+# drop-in headers; those tests are skipped unless this variable names the tree.
+REFERENCE_ROOT = os.environ.get("MSOSM_REFERENCE_ROOT")
+
+
+def cuda_compile_flags() -> list[str]:
+    """g++ flags for a program that includes cuda_runtime.h and links the CUDA runtime."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    root = Path(nvcc).resolve().parent.parent
+    return ["-I", str(root / "include"), "-L", str(root / "lib64"), "-lcudart", f"-Wl,-rpath,{root / 'lib64'}"]
 
 
 def pytest_configure(config):

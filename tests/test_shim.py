@@ -3,8 +3,9 @@
 * A program written against the reference's class interface compiles and links
   against the engine library, and its host-only parts (planning, psrdada
   parsing) run without a GPU.
-* Where the reference tree exists, the reference's own msosm_psrdada.cpp main
-  compiles and links unchanged against the shim.
+* Where the reference tree is given (MSOSM_REFERENCE_ROOT), each of the reference's
+  five programs (msosm_psrdada.cpp, msosm_save_simulated.cpp and the three benchmark
+  mains) compiles and links unchanged against the shim.
 """
 from __future__ import annotations
 
@@ -14,6 +15,8 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+
+from conftest import REFERENCE_ROOT, cuda_compile_flags
 
 ROOT = Path(__file__).resolve().parents[1]
 COMPAT = ROOT / "include" / "compat"
@@ -70,7 +73,7 @@ def shim_program(tmp_path_factory, eng):
     src.write_text(PROGRAM)
     exe = d / "prog"
     r = subprocess.run([_gxx(), "-std=c++17", "-O1", "-I", str(COMPAT), str(src), "-L", str(LIBDIR), "-lmsosm_gb300",
-                        f"-Wl,-rpath,{LIBDIR}", "-o", str(exe)], capture_output=True, text=True)
+                        f"-Wl,-rpath,{LIBDIR}", *cuda_compile_flags(), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
 
@@ -127,10 +130,16 @@ def test_psrdada_rejects_truncated_header(shim_program, tmp_path):
     assert r.returncode != 0 and "header" in r.stderr
 
 
-@pytest.mark.skipif(not Path("/root/reference/msosm_psrdada.cpp").exists(), reason="reference tree not present")
-def test_reference_main_compiles_against_shim(tmp_path, eng):
-    exe = tmp_path / "msosm_psrdada"
-    r = subprocess.run([_gxx(), "-std=c++17", "-O1", "-I", str(COMPAT), "/root/reference/msosm_psrdada.cpp", "-L",
-                        str(LIBDIR), "-lmsosm_gb300", f"-Wl,-rpath,{LIBDIR}", "-o", str(exe)],
-                       capture_output=True, text=True)
+REFERENCE_MAINS = ["msosm_psrdada.cpp", "msosm_save_simulated.cpp", "benchmark/check_msosm.cpp",
+                   "benchmark/check_osm.cpp", "benchmark/test_msosm_speed.cpp"]
+
+
+@pytest.mark.skipif(not REFERENCE_ROOT, reason="MSOSM_REFERENCE_ROOT does not name the reference tree")
+@pytest.mark.parametrize("main", REFERENCE_MAINS)
+def test_reference_main_compiles_against_shim(tmp_path, eng, main):
+    src = Path(REFERENCE_ROOT) / main
+    assert src.exists(), src
+    exe = tmp_path / Path(main).stem
+    r = subprocess.run([_gxx(), "-std=c++17", "-O1", "-I", str(COMPAT), str(src), "-L", str(LIBDIR), "-lmsosm_gb300",
+                        f"-Wl,-rpath,{LIBDIR}", *cuda_compile_flags(), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
