@@ -1,9 +1,13 @@
 // Tile FFT building blocks for the MS-OSM engine (sm_103a).
 //
 // A CTA transforms COLS independent length-N sequences ("columns") held in
-// shared memory.  Stages are Stockham autosort stages of radix 8 (then 4 or 2
-// to finish), each thread owning BPT butterflies per stage with all R inputs in
-// registers.  The first stage may read straight from global memory through a
+// shared memory.  Stages are Stockham autosort stages, each thread owning BPT
+// butterflies per stage with all R inputs in registers.  The default plan takes
+// radix-8 stages (then 4 or 2 to finish); the "big" plan used by the persistent
+// inverse transform takes two register stages of radix 16/32 (N = 512: 16 x 32,
+// N = 1024: 32 x 32, N = 256: 16 x 16, N = 2048: 16 x 8 x 16; see StageRadix).
+// Register DFTs of radix 16 and 32 are composites of radix-8/4/2 kernels with
+// compile-time twiddle constants.  The first stage may read straight from global memory through a
 // loader functor and the last stage may hand its outputs to an epilogue functor
 // instead of shared memory, so a pass touches shared memory only between stages.
 //

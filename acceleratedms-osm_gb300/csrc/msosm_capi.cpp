@@ -558,7 +558,7 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
     const int L = ilog2(F);
     h->g = Geom{L, (int)F, M, 1 << (L / 2), 1 << (L - L / 2)};
 
-    // segmentation of every DM (msosm_gpu_batch.cpp:150-157)
+    // segmentation of every DM (msosm_gpu_batch.cpp:54-61)
     const size_t DF = (size_t)h->D * F;
     std::vector<uint16_t> delays(DF, 0);
     h->dc.assign(h->D, 0);
@@ -585,7 +585,7 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
         fbs += batch - fbs % batch;
     h->fbs = std::max(fbs, batch);
 
-    // responses (msosm_gpu_batch.cpp:183-189) on host threads, FP64 inside
+    // responses (msosm_gpu_batch.cpp:86-93) on host threads, FP64 inside
     std::vector<float> H(2 * DF);
     const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
     msosm::plan_responses(h->bw, h->f0, h->dms.data(), h->D, M, H.data(), threads);
@@ -920,7 +920,7 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
             return h->cuda_fail(e, "inverse transform launch (pass 2)");
     }
     if (h->fold)
-        h->fold->t_start += (double)((size_t)h->B * h->M) * h->fold->dt; // fold_gpu.cpp:96
+        h->fold->t_start += (double)((size_t)h->B * h->M) * h->fold->dt; // fold_gpu.cpp:53
     if (h->writer)
     {
         std::string werr;
@@ -1404,7 +1404,7 @@ extern "C" int msosm_fold_create(float period, float fs, unsigned long size, uns
     f->P = (double)period;      // period_seconds (fold_gpu.cpp:9)
     f->dt = 1.0 / (double)fs;   // fold_data_phase (fold_gpu.cpp:50)
     f->size = size;
-    // period_samples = (unsigned long)(float)(period*fs) (fold_gpu.cpp:10-15)
+    // period_samples = (unsigned long)(float)(period*fs) (fold_gpu.cpp:10-16)
     const float psf = period * fs;
     f->K = time_bin ? time_bin : (unsigned long)psf;
     f->S = num_series;

@@ -49,7 +49,7 @@ __device__ __forceinline__ float2 load_sample(const void *__restrict__ in, size_
     }
 }
 
-// discardSamplesToUint16 epilogue (gpu/gpu_kernel.cu:445-459): round-to-nearest,
+// discardSamplesToUint16 epilogue (gpu/gpu_kernel.cu:398-413): round-to-nearest,
 // offset 32768 for non-zero values, packed (y << 16) | x.
 __device__ __forceinline__ uint32_t encode_u16(float2 v)
 {

@@ -1,7 +1,7 @@
 // Stand-alone intensity + phase fold (Fold_GPU, folding/fold_gpu.cpp:27-60).
 //
-// Replaces calculateIntensity / calculateIntensity_single (gpu/gpu_kernel.cu:477-507),
-// foldDataPhase (gpu_kernel.cu:509-543) and computeFoldedData (gpu_kernel.cu:545-565)
+// Replaces calculateIntensity / calculateIntensity_single (gpu/gpu_kernel.cu:430-460),
+// foldDataPhase (gpu_kernel.cu:462-496) and computeFoldedData (gpu_kernel.cu:498-518)
 // for callers that fold the processor's complex output themselves (the 2-pol
 // path and the reference-shaped Fold_GPU object).  The intensity is computed on
 // the fly -- no intensity buffer -- and samples are binned with the same Q0.64

@@ -1,10 +1,10 @@
 // Per-DM inverse transforms of the MS-OSM stream.
 //
 // Replaces, for every (DM d, window b), the reference's gatherMultiply_kernel
-// (gpu/gpu_kernel.cu:152-257), the batched cufftExecC2C inverse
-// (msosm_gpu_batch.cpp:292-295) and discardSamples / discardSamplesToUint16
-// (gpu_kernel.cu:393-475), plus, when folding, calculateIntensity_single and
-// foldDataPhase (gpu_kernel.cu:485-543).
+// (gpu/gpu_kernel.cu:106-210), the batched cufftExecC2C inverse
+// (msosm_gpu_batch.cpp:196-199) and discardSamples / discardSamplesToUint16
+// (gpu_kernel.cu:346-376, 398-428), plus, when folding, calculateIntensity_single and
+// foldDataPhase (gpu_kernel.cu:438-444, 462-496).
 //
 //   pass 1 (column n1): x[n] = ring[(rbi + b - delay_d[n]) mod fbs][n] * H_d[n]
 //           for n = n1 + N1*n2 -- the delayed-bin gather and the response

@@ -232,7 +232,7 @@ struct PEpilogue
                 out_pow[o] = x.x * x.x + x.y * x.y;
             if constexpr ((MODE & OUT_PAIR) != 0)
             {
-                // 2-pol intensity sqrt(|a|^2 + |b|^2) (calculateIntensity, gpu_kernel.cu:430-440)
+                // 2-pol intensity sqrt(|a|^2 + |b|^2) (calculateIntensity_kernel, gpu_kernel.cu:430-436)
                 s_p[k1h * COLS + col] = sqrtf(__ldcs(pair_pow + o) + (x.x * x.x + x.y * x.y));
             }
             else if constexpr ((MODE & OUT_FOLD) != 0)

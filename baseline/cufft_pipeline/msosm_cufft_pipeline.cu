@@ -3,7 +3,7 @@
 //
 // Per call of B windows (dedispersion/msosm/msosm_gpu_batch.cpp:178-236, fold mode):
 //   1. the B*M new samples follow the previous call's last M samples in one window buffer
-//      (increment_fft_input, msosm_gpu_batch.cpp:153-166);
+//      (increment_fft_input, msosm_gpu_batch.cpp:153-165);
 //   2. one batched cuFFT forward transform of B overlapping windows (idist = M) into B slots
 //      of the spectra ring (msosm_gpu_batch.cpp:100-107, 191);
 //   3. per DM chunk: the delayed-bin gather x response (gatherMultiply_kernel,

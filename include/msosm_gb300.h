@@ -9,7 +9,7 @@
  *
  * Every function returns an int status (MSOSM_OK = 0).  Nothing here calls
  * exit() or resets the device, unlike the reference's CUDA_CHECK / destructor
- * (gpu/include/gpu_common.cuh:42-62, dedispersion/msosm/msosm_gpu_batch.cpp:252-260).
+ * (gpu/include/gpu_common.cuh:42-62, dedispersion/msosm/msosm_gpu_batch.cpp:252-255).
  * msosm_last_error() returns the message of a handle's last failure.
  *
  * Threading: a handle is driven by one host thread at a time (the reference's
@@ -242,7 +242,7 @@ int msosm_fold_accumulate_cross(msosm_fold_t *f, const void *x, const void *dx, 
 
 /* ---- checkpoint / resume -------------------------------------------------------
  * No counterpart in the reference (its stream state lives only in device memory,
- * msosm_gpu_batch.cpp:146-148, 218-221).  The state of a stream is the previous
+ * msosm_gpu_batch.cpp:50-52, 113-125).  The state of a stream is the previous
  * call's last M samples, the ring of past spectra and the call counter; it does
  * not depend on the DM list, so it can be restored into any handle with the same
  * M, batch and ring size.  msosm_state_bytes gives the buffer size; save/load copy
@@ -271,7 +271,7 @@ int osm_create(float bw, float dm, float f0, msosm_t **out);
  * msosm_fold_accumulate replaces calculate_intensity(pol1[, pol2]) followed by
  *   fold_data_phase() (fold_gpu.cpp:27-54): pol1/pol2 are device complex64
  *   series of num_series*size samples; pol2 NULL gives |a|^2, otherwise
- *   sqrt(|a|^2+|b|^2) (gpu/gpu_kernel.cu:477-491); zero samples are skipped; the
+ *   sqrt(|a|^2+|b|^2) (gpu/gpu_kernel.cu:430-444); zero samples are skipped; the
  *   fold's time origin advances by size/fs per call.
  * msosm_fold_read replaces get_folded_data() (fold_gpu.cpp:56-60): folded mean
  *   per bin (float, [num_series][time_bin]) and optionally the raw double sums
@@ -292,7 +292,7 @@ int msosm_attach_fold(msosm_t *h, msosm_fold_t *f);
  * fold_gpu.cpp:27-60, for two processors of the same plan): `first` writes |a|^2 of
  * every output sample into a buffer the fold owns (num_series*size floats), and every
  * msosm_process of `second` folds sqrt(|a|^2 + |b|^2) of the same samples -- the
- * reference's 2-pol intensity (gpu_kernel.cu:430-440) -- with no complex series written.
+ * reference's 2-pol intensity (gpu_kernel.cu:430-436) -- with no complex series written.
  * Per step: msosm_process(first, pol_a) then msosm_process(second, pol_b) on one stream.
  * Both handles: same DMs, batch and fftpoint (>= 65536), MSOSM_OUT_NONE. f = NULL
  * detaches both. */

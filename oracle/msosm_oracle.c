@@ -381,7 +381,7 @@ static uint32_t orc_f2u_rn(float s)
     return (uint32_t)rintf(s);
 }
 
-/* discardSamplesToUint16_kernel epilogue, gpu/gpu_kernel.cu:445-459, applied to
+/* discardSamplesToUint16_kernel epilogue, gpu/gpu_kernel.cu:398-413, applied to
  * already-scaled float values: u = rn(v + 32768*(v!=0)), packed (y<<16)|x. */
 void orc_encode_u16(const float *in, size_t n, uint32_t *out)
 {
@@ -398,14 +398,14 @@ void orc_encode_u16(const float *in, size_t n, uint32_t *out)
 /* folding                                                                   */
 /* ------------------------------------------------------------------------ */
 
-/* calculateIntensity_single_kernel (gpu_kernel.cu:485-491): |a|^2, no sqrt */
+/* calculateIntensity_single_kernel (gpu_kernel.cu:438-444): |a|^2, no sqrt */
 void orc_intensity1(const float *a, size_t n, float *out)
 {
     for (size_t i = 0; i < n; i++)
         out[i] = a[2 * i] * a[2 * i] + a[2 * i + 1] * a[2 * i + 1];
 }
 
-/* calculateIntensity_kernel (gpu_kernel.cu:477-483): sqrt(|a|^2+|b|^2) */
+/* calculateIntensity_kernel (gpu_kernel.cu:430-436): sqrt(|a|^2+|b|^2) */
 void orc_intensity2(const float *a, const float *b, size_t n, float *out)
 {
     for (size_t i = 0; i < n; i++)
@@ -413,7 +413,7 @@ void orc_intensity2(const float *a, const float *b, size_t n, float *out)
                        b[2 * i + 1] * b[2 * i + 1]);
 }
 
-/* foldDataPhase_kernel (gpu_kernel.cu:509-532) on the host. */
+/* foldDataPhase_kernel (gpu_kernel.cu:462-485) on the host. */
 void orc_fold(const float *inten, size_t n, unsigned long K, double t_start, double dt, double period,
               double *sum, unsigned long long *cnt)
 {
@@ -441,7 +441,7 @@ unsigned long orc_fold_bin(double t_start, double dt, double period, unsigned lo
     return bin >= K ? K - 1 : bin;
 }
 
-/* computeFoldedData_kernel (gpu_kernel.cu:545-555) */
+/* computeFoldedData_kernel (gpu_kernel.cu:498-508) */
 void orc_fold_finalize(const double *sum, const unsigned long long *cnt, unsigned long K, float *out)
 {
     for (unsigned long b = 0; b < K; b++)

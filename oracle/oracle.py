@@ -8,10 +8,10 @@ The functions restate the reference (joezhouchenye/AcceleratedMS-OSM):
   plan()        Prepare_MSOSM ctor + calculate_min_order + initialize_uint16's
                 choice of M + segmentation + generate_dedisp_params
                 (dedispersion/msosm/msosm_prepare.cpp:3-284,
-                 dedispersion/msosm/msosm_gpu_batch.cpp:32-44,150-189)
+                 dedispersion/msosm/msosm_gpu_batch.cpp:32-44,54-61,86-93,113-117)
   Msosm         the streaming processor (msosm_gpu_batch.cpp:153-236 with the
                 kernels of gpu/gpu_kernel.cu), FP64 or FP32
-  fold()        foldDataPhase (gpu/gpu_kernel.cu:509-532)
+  fold()        foldDataPhase (gpu/gpu_kernel.cu:462-485)
 """
 from __future__ import annotations
 
@@ -25,6 +25,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "lib" / "libmsosm_oracle.so"
 REF_LIB_PATH = HERE / "_ref" / "libmsosm_ref.so"
+REF_SEG_LIB_PATH = HERE / "_ref" / "libmsosm_ref_seg.so"
+# the reference source tree, for building oracle/_ref; only where it is given
+REFERENCE_ROOT_ENV = "MSOSM_REFERENCE_ROOT"
 
 _lib = None
 
@@ -37,9 +40,11 @@ def build(quiet: bool = True) -> Path:
     return LIB_PATH
 
 
-def build_ref(ref_root: str = "/root/reference") -> Path | None:
-    """Compile the reference's own planning sources (only where that tree exists)."""
-    if not Path(ref_root).is_dir():
+def build_ref(ref_root: str | None = None) -> Path | None:
+    """Compile the reference's own planning sources and build_segments (only where the
+    tree is given, as an argument or through MSOSM_REFERENCE_ROOT)."""
+    ref_root = ref_root or os.environ.get(REFERENCE_ROOT_ENV)
+    if not ref_root or not Path(ref_root).is_dir():
         return None
     out = subprocess.run(["make", "-C", str(HERE), "ref", f"REF_ROOT={ref_root}"],
                          capture_output=True, text=True)
@@ -186,7 +191,7 @@ class Plan:
         for i, d in enumerate(self.dms):
             self.delays[i], self.dc[i] = segmentation(self.bw, self.f0, float(d), int(self.nd[i]), self.M)
         self.delaycount = int(self.dc.max()) if len(self.dc) else 0
-        fbs = self.delaycount + batch - 1  # msosm_gpu_batch.cpp:113-118
+        fbs = self.delaycount + batch - 1  # msosm_gpu_batch.cpp:113-117
         if fbs % batch:
             fbs += batch - fbs % batch
         self.fbs = max(fbs, batch)
@@ -352,6 +357,17 @@ def ref_plan(bw, f0, dms, fftpoint=0, want_delays=True, want_H=True):
     R.ref_msosm_tables(bw, f0, _p(dms), n, M, _p(dc), _p(dcmax),
                        _p(delays) if want_delays else None, _p(H) if want_H else None)
     return dict(nd=nd_, M_min=int(mmin[0]), M=M, dc=dc, delaycount=int(dcmax[0]), delays=delays, H=H)
+
+
+def ref_build_segments(delay: np.ndarray) -> np.ndarray:
+    """The reference's MSOSM_GPU_BATCH::build_segments on one delay map: (n, 3) int32
+    (start, len, group)."""
+    L = C.CDLL(str(REF_SEG_LIB_PATH))
+    L.ref_build_segments.argtypes = [P, I, P, I]
+    d = np.ascontiguousarray(delay, dtype=np.int32)
+    out = np.zeros((len(d), 3), np.int32)
+    n = L.ref_build_segments(_p(d), len(d), _p(out), len(d))
+    return out[:n].copy()
 
 
 def ref_osm_plan(bw, dm, f0, fftpoint=0, want_H=True):

@@ -5,7 +5,7 @@
  * and once with ORC_REAL=float (the FP32 CPU port used as the timed CPU baseline).
  * It stands in for the FFTW / cuFFT transforms the reference calls:
  *   - FFTW_BACKWARD/FFTW_FORWARD in dedispersion/msosm/msosm_prepare.cpp:200-221
- *   - cufftExecC2C forward/inverse in dedispersion/msosm/msosm_gpu_batch.cpp:287,294
+ *   - cufftExecC2C forward/inverse in dedispersion/msosm/msosm_gpu_batch.cpp:191,196-199
  * Sign convention follows FFTW/cuFFT: sign=-1 forward, sign=+1 inverse,
  * both unnormalised.  Twiddles are always computed in double and rounded.
  */

@@ -6,19 +6,19 @@
  * "port" timed as the CPU baseline.  Nothing in the product links this file.
  *
  * Semantics restated from the reference's GPU processor:
- *   ring / overlap bookkeeping  dedispersion/msosm/msosm_gpu_batch.cpp:249-272
+ *   ring / overlap bookkeeping  dedispersion/msosm/msosm_gpu_batch.cpp:153-176
  *     - complex input buffer of (B+1)*M samples, first M = previous call's tail,
- *       zero before the first call (msosm_gpu_batch.cpp:146-148, 251-258)
+ *       zero before the first call (msosm_gpu_batch.cpp:50-52, 153-165)
  *     - forward spectra ring of fbs slots; call s writes slots
- *       rbi..rbi+B-1 with rbi = (s*B) mod fbs (msosm_gpu_batch.cpp:263-271)
- *   forward FFT: B windows of F=2M samples, hop M (msosm_gpu_batch.cpp:196-203,287)
- *   gather x multiply: gpu/gpu_kernel.cu:152-239
+ *       rbi..rbi+B-1 with rbi = (s*B) mod fbs (msosm_gpu_batch.cpp:167-176)
+ *   forward FFT: B windows of F=2M samples, hop M (msosm_gpu_batch.cpp:100-107, 189-191)
+ *   gather x multiply: gpu/gpu_kernel.cu:106-192
  *       x[n] = ring[((rbi + b - delay[n]) mod fbs)][n] * H[n]   (no 1/F here)
- *   inverse FFT (unnormalised): msosm_gpu_batch.cpp:231,292-295
- *   discard: gpu/gpu_kernel.cu:393-415  out[(d*B+b)*M+o] = y[M+o] * (1/(2M))
- *   fold: gpu/gpu_kernel.cu:485-532 and folding/fold_gpu.cpp:91-97
+ *   inverse FFT (unnormalised): msosm_gpu_batch.cpp:135,196-199
+ *   discard: gpu/gpu_kernel.cu:346-368  out[(d*B+b)*M+o] = y[M+o] * (1/(2M))
+ *   fold: gpu/gpu_kernel.cu:430-496 and folding/fold_gpu.cpp:48-54
  * The ring is zeroed here (the reference leaves it uninitialised,
- * msosm_gpu_batch.cpp:218), so warm-up outputs are deterministic.
+ * msosm_gpu_batch.cpp:122), so warm-up outputs are deterministic.
  */
 #ifndef ORC_REAL
 #error "define ORC_REAL before including orc_msosm_impl.h"
@@ -125,15 +125,15 @@ static void ORC_FN(inv_task)(void *ctx, long job, int tid)
     for (int n = 0; n < F; n++)
     {
         int slot = h->rbi + b - dl[n];
-        slot = ((slot % fbs) + fbs) % fbs; /* gpu_kernel.cu:188-189 */
+        slot = ((slot % fbs) + fbs) % fbs; /* gpu_kernel.cu:141-142 */
         const ORC_REAL *sp = h->ring + 2 * ((size_t)slot * F + n);
         ORC_REAL vr = sp[0], vi = sp[1];
         ORC_REAL pr = Hd[2 * n], pi_ = Hd[2 * n + 1];
-        x[2 * n] = vr * pr - vi * pi_; /* gpu_kernel.cu:233-234 */
+        x[2 * n] = vr * pr - vi * pi_; /* gpu_kernel.cu:183-184 */
         x[2 * n + 1] = vr * pi_ + vi * pr;
     }
     ORC_FN(orc_fft_exec)(h->pb, x, sc);
-    const ORC_REAL scale = (ORC_REAL)1 / (ORC_REAL)(2 * M); /* gpu_kernel.cu:405 */
+    const ORC_REAL scale = (ORC_REAL)1 / (ORC_REAL)(2 * M); /* gpu_kernel.cu:358 */
     ORC_REAL *o = h->out ? h->out + 2 * ((size_t)(d * B + b) * M) : NULL;
     double *fs = h->fsum ? h->fsum + ((size_t)tid * h->D + d) * h->K : NULL;
     unsigned long long *fc = h->fcnt ? h->fcnt + ((size_t)tid * h->D + d) * h->K : NULL;
@@ -147,10 +147,10 @@ static void ORC_FN(inv_task)(void *ctx, long job, int tid)
         }
         if (fs)
         {
-            /* calculateIntensity_single_kernel: |a|^2 in float (gpu_kernel.cu:485-491) */
+            /* calculateIntensity_single_kernel: |a|^2 in float (gpu_kernel.cu:438-444) */
             float fx = (float)yr, fy = (float)yi;
             float val = fx * fx + fy * fy;
-            if (val == 0.0f) /* gpu_kernel.cu:521-522 */
+            if (val == 0.0f) /* gpu_kernel.cu:474-476 */
                 continue;
             double t = h->t_start + (double)((size_t)b * M + i) * h->dt;
             double phase = fmod(t / h->period, 1.0);
@@ -168,7 +168,7 @@ static void ORC_FN(inv_task)(void *ctx, long job, int tid)
 void ORC_API(msosm_process)(ORC_FN(orc_msosm) * h, const ORC_REAL *in, ORC_REAL *out)
 {
     const int M = h->M, B = h->B;
-    /* overlap: previous tail is buf[B*M..(B+1)*M) -> buf[0..M) (msosm_gpu_batch.cpp:251-258) */
+    /* overlap: previous tail is buf[B*M..(B+1)*M) -> buf[0..M) (msosm_gpu_batch.cpp:155-162) */
     if (h->step > 0)
         memmove(h->buf, h->buf + 2 * (size_t)B * M, sizeof(ORC_REAL) * 2 * M);
     memcpy(h->buf + 2 * (size_t)M, in, sizeof(ORC_REAL) * 2 * (size_t)B * M);
@@ -178,7 +178,7 @@ void ORC_API(msosm_process)(ORC_FN(orc_msosm) * h, const ORC_REAL *in, ORC_REAL 
     orc_parallel_for((long)h->D * B, h->nthreads, ORC_FN(inv_task), h);
     h->out = NULL;
     if (h->fsum)
-        h->t_start += (double)((size_t)B * M) * h->dt; /* fold_gpu.cpp:96 */
+        h->t_start += (double)((size_t)B * M) * h->dt; /* fold_gpu.cpp:53 */
     h->step++;
 }
 

@@ -2,13 +2,13 @@
 
 Run in a container where the reference tree exists:
 
-    python tests/golden/make_golden.py [--ref-root /root/reference]
+    python tests/golden/make_golden.py --ref-root <reference tree> [--segments-only]
 
 It compiles the reference's dedispersion/msosm/msosm_prepare.cpp and
 dedispersion/overlap_save/osm_prepare.cpp unmodified (oracle/Makefile target
 `ref`, against a project-written FFTW-API shim, since FFTW is not installed),
 drives them the way MSOSM_GPU_BATCH::initialize_uint16 and
-OSM_GPU_BATCH::initialize_uint16 do (msosm_gpu_batch.cpp:12-189,
+OSM_GPU_BATCH::initialize_uint16 do (msosm_gpu_batch.cpp:12-93,
 osm_gpu_batch.cpp:19-45) and writes what they compute:
 
   plan_cases.json   Nd per DM, M_min, M, delaycount per DM, the processor-wide
@@ -18,6 +18,11 @@ osm_gpu_batch.cpp:19-45) and writes what they compute:
                     a strided sample + L2 norm for the large ones
   osm_cases.json    Prepare_OSM's Nd / M_min / M for the OSM cases (+ H samples
                     in response.npz)
+  segment_cases.json  the reference's own MSOSM_GPU_BATCH::build_segments
+                    (msosm_gpu_batch.cpp:262-295, compiled unmodified against stub
+                    kernel headers) on every delay map above: segment count and
+                    SHA-256 of the int32 (start, len, group) triples per DM, and the
+                    full triples of the small cases
 
 The fixtures travel with the repository; the GPU machine never needs the reference.
 """
@@ -77,12 +82,40 @@ def runs(delay: np.ndarray):
     return [[int(s), int(e - s), int(d[s])] for s, e in zip(starts, ends)]
 
 
+def segment_fixtures():
+    import hashlib
+
+    out = {}
+    for name, bw, fc, dms, fftpoint, full_h in msosm_cases():
+        bw32 = np.float32(bw)
+        f0 = np.float32(np.float32(fc) - np.float32(bw) / np.float32(2))
+        r = O.ref_plan(bw32, f0, np.asarray(dms, np.float32), fftpoint, want_delays=True, want_H=False)
+        per = []
+        for i in range(len(dms)):
+            if r["dc"][i] == 0:  # DM 0: the reference leaves the delay map unset
+                per.append(None)
+                continue
+            seg = O.ref_build_segments(r["delays"][i])
+            e = dict(count=int(len(seg)), sha256=hashlib.sha256(seg.astype("<i4").tobytes()).hexdigest())
+            if full_h:
+                e["triples"] = seg.tolist()
+            per.append(e)
+        out[name] = per
+        print(f"{name}: segments per DM {[p['count'] for p in per if p][:4]}...")
+    (OUT / "segment_cases.json").write_text(json.dumps(out, separators=(",", ":")))
+    print("segment_cases.json", (OUT / "segment_cases.json").stat().st_size, "bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=None, help="the reference tree (default: $MSOSM_REFERENCE_ROOT)")
+    ap.add_argument("--segments-only", action="store_true")
     args = ap.parse_args()
     if O.build_ref(args.ref_root) is None:
-        raise SystemExit(f"reference tree not found at {args.ref_root}")
+        raise SystemExit("give the reference tree with --ref-root or MSOSM_REFERENCE_ROOT")
+    segment_fixtures()
+    if args.segments_only:
+        return
     plans = {}
     arrays = {}
     for name, bw, fc, dms, fftpoint, full_h in msosm_cases():

@@ -169,3 +169,31 @@ def test_fold_known_answer(orc):
     np.testing.assert_allclose(s, [6, 2, 10, 12])
     np.testing.assert_array_equal(c, [2, 1, 2, 2])  # the zero sample is skipped
     np.testing.assert_allclose(orc.fold_finalize(s, c), [3, 2, 5, 6])
+
+
+def test_build_segments_matches_the_reference(orc, golden_plans):
+    """The oracle's build_segments restatement against the reference's own
+    MSOSM_GPU_BATCH::build_segments (msosm_gpu_batch.cpp:262-295) run on the same
+    delay maps (tests/golden/segment_cases.json): same triples, every DM of every case."""
+    import hashlib
+    import json
+
+    from conftest import GOLDEN, expand_runs
+
+    ref = json.loads((GOLDEN / "segment_cases.json").read_text())
+    checked = 0
+    for name, per in ref.items():
+        case = golden_plans[name]
+        F = 2 * case["M"]
+        for i, e in enumerate(per):
+            if e is None:
+                assert case["delay_runs"][i] is None
+                continue
+            st, ln, gr = orc.build_segments(expand_runs(case["delay_runs"][i], F))
+            tri = np.stack([st, ln, gr], axis=1).astype("<i4")
+            assert len(tri) == e["count"], (name, i)
+            assert hashlib.sha256(tri.tobytes()).hexdigest() == e["sha256"], (name, i)
+            if "triples" in e:
+                assert tri.tolist() == e["triples"]
+            checked += 1
+    assert checked == 591  # all DMs but the many-DM grid's DM 0
