@@ -1,15 +1,25 @@
 // Drop-in replacement for psrdada/include/psrdada.h (header-only).
 //
-// PSRDADA file reader with the reference's interface (psrdada.h:16-43,
-// psrdada.cpp:3-127): a 4096-byte ASCII header (BW, FREQ, NBIT, NCHAN, NDIM,
-// NPOL, one "KEY value" per line), then frames of 2048 samples per polarisation,
-// polarisations interleaved frame by frame.  NBIT 16 reads uint16_pair samples
-// into pol1_in/pol2_in as the reference does; NBIT 8 (new) reads int8 I/Q pairs
-// into pol1_i8/pol2_i8 (2 bytes per sample) for processors initialised with
-// MSOSM_IN_I8.  Unlike the reference, failures throw std::runtime_error instead
-// of calling exit(1), and short reads are reported by readSamples()'s return.
+// The interface is the reference's PSRDADA class (psrdada.h:16-43: constructor,
+// initBuffer, readSamples and the public members), written from the DADA file
+// layout rather than from the reference's implementation:
+//   * the file starts with a 4096-byte ASCII header block, NUL-padded, holding one
+//     "KEY value" pair per line (whitespace-separated); the keys used here are BW
+//     (MHz), FREQ (centre, MHz), NBIT, NCHAN, NDIM and NPOL; other keys are ignored;
+//   * the data follow in frames of 2048 samples per polarisation, the polarisations'
+//     frames interleaved (pol 1 frame k, pol 2 frame k, pol 1 frame k+1, ...);
+//   * NBIT 16 samples are uint16_pair offset-binary I/Q (read into pol1_in/pol2_in);
+//     NBIT 8 (an addition) are int8 I/Q pairs, 2 bytes per sample (pol1_i8/pol2_i8),
+//     for processors initialised with MSOSM_IN_I8.
+// initBuffer(n) sizes n samples per polarisation per read (a whole number of frames)
+// and sets readCount, the number of whole reads the data hold; readSamples() fills
+// the buffers with the next read and returns false on a short read.  The folded-
+// profile file name is the input name with its extension replaced by
+// "_dedisp_folded.txt".  Failures throw std::runtime_error (the reference exits).
 #pragma once
 #include "globals.h"
+
+#include <map>
 #include <sstream>
 #include <stdexcept>
 #include <utility>
@@ -20,45 +30,26 @@ auto constexpr frameSamples = 2048;
 class PSRDADA
 {
   public:
-    explicit PSRDADA(string filename)
+    explicit PSRDADA(string filename) : infileName(std::move(filename))
     {
-        infileName = filename;
-        infile.open(filename, ios::binary | ios::ate);
-        if (!infile.is_open())
-            throw std::runtime_error("Cannot open file: " + filename);
+        infile.open(infileName, ios::binary);
+        if (!infile)
+            throw std::runtime_error("PSRDADA: cannot open " + infileName);
+        infile.seekg(0, ios::end);
         filesize = (unsigned long)infile.tellg();
         infile.seekg(0, ios::beg);
-        outfileName = filename.substr(0, filename.find_last_of('.')) + "_dedisp_folded.txt";
         if (filesize < (unsigned long)blockSize)
-            throw std::runtime_error("file shorter than the 4096-byte header: " + filename);
+            throw std::runtime_error("PSRDADA: " + infileName + " is shorter than the 4096-byte header block");
         infile.read(headerBuffer, blockSize);
-        string header(headerBuffer, blockSize);
-        header.erase(std::remove(header.begin(), header.end(), '\0'), header.end());
-        istringstream iss(header);
-        string ln;
-        while (getline(iss, ln))
-        {
-            auto kv = split(ln);
-            try
-            {
-                if (kv.first == "BW")
-                    bw = stof(kv.second);
-                else if (kv.first == "FREQ")
-                    fc = stof(kv.second);
-                else if (kv.first == "NBIT")
-                    nbit = stoi(kv.second);
-                else if (kv.first == "NCHAN")
-                    nchan = stoi(kv.second);
-                else if (kv.first == "NDIM")
-                    ndim = stoi(kv.second);
-                else if (kv.first == "NPOL")
-                    npol = stoi(kv.second);
-            }
-            catch (const std::exception &)
-            {
-                throw std::runtime_error("bad header value for " + kv.first);
-            }
-        }
+        const std::map<string, string> keys = parse_header(headerBuffer, blockSize);
+        bw = number<float>(keys, "BW", bw);
+        fc = number<float>(keys, "FREQ", fc);
+        nbit = number<int>(keys, "NBIT", nbit);
+        nchan = number<int>(keys, "NCHAN", nchan);
+        ndim = number<int>(keys, "NDIM", ndim);
+        npol = number<int>(keys, "NPOL", npol);
+        const size_t dot = infileName.find_last_of('.');
+        outfileName = (dot == string::npos ? infileName : infileName.substr(0, dot)) + "_dedisp_folded.txt";
         if (verbose)
         {
             cout << "Bandwidth: " << bw << " MHz" << endl;
@@ -69,21 +60,22 @@ class PSRDADA
     }
     ~PSRDADA()
     {
-        infile.close();
         delete[] pol1_in;
         delete[] pol2_in;
         delete[] pol1_i8;
         delete[] pol2_i8;
     }
     size_t sample_bytes() const { return nbit == 8 ? 2 : sizeof(uint16_pair); }
+
     void initBuffer(size_t n)
     {
-        if (n % frameSamples != 0)
-            throw std::runtime_error("n must be a multiple of frameSamples (2048)");
-        if (npol != 1 && npol != 2)
-            throw std::runtime_error("Unsupported polarization number: " + to_string(npol));
-        if (nbit != 16 && nbit != 8)
-            throw std::runtime_error("Unsupported NBIT: " + to_string(nbit));
+        if (npol < 1 || npol > 2)
+            throw std::runtime_error("PSRDADA: NPOL " + to_string(npol) + " is not supported (1 or 2)");
+        if (nbit != 8 && nbit != 16)
+            throw std::runtime_error("PSRDADA: NBIT " + to_string(nbit) + " is not supported (8 or 16)");
+        if (n == 0 || n % frameSamples)
+            throw std::runtime_error("PSRDADA: samples per read must be a whole number of 2048-sample frames");
+        frameCount = (int)(n / frameSamples);
         if (nbit == 16)
         {
             pol1_in = new uint16_pair[n];
@@ -94,22 +86,19 @@ class PSRDADA
             pol1_i8 = new int8_t[2 * n];
             pol2_i8 = new int8_t[2 * n];
         }
-        frameCount = (int)(n / frameSamples);
-        readCount = (unsigned long)((filesize - blockSize) / (npol * n * sample_bytes()));
+        const unsigned long per_read = (unsigned long)npol * n * sample_bytes();
+        readCount = (filesize - blockSize) / per_read;
     }
-    // Reads frameCount frames per polarisation; false on a short read.
+
     bool readSamples()
     {
-        const size_t fb = frameSamples * sample_bytes();
-        char *p1 = nbit == 16 ? (char *)pol1_in : (char *)pol1_i8;
-        char *p2 = nbit == 16 ? (char *)pol2_in : (char *)pol2_i8;
-        for (int i = 0; i < frameCount; i++)
-        {
-            if (!infile.read(p1 + i * fb, fb))
-                return false;
-            if (npol == 2 && !infile.read(p2 + i * fb, fb))
-                return false;
-        }
+        char *dst[2] = {nbit == 16 ? (char *)pol1_in : (char *)pol1_i8,
+                        nbit == 16 ? (char *)pol2_in : (char *)pol2_i8};
+        const std::streamsize frame = (std::streamsize)(frameSamples * sample_bytes());
+        for (int k = 0; k < frameCount; k++)
+            for (int p = 0; p < npol; p++)
+                if (!infile.read(dst[p] + (size_t)k * frame, frame))
+                    return false;
         return true;
     }
 
@@ -130,14 +119,37 @@ class PSRDADA
     int frameCount = 0;
 
   private:
-    static pair<string, string> split(const string &input)
+    // "KEY value" lines of the NUL-padded ASCII block; the first token is the key,
+    // the second the value
+    static std::map<string, string> parse_header(const char *buf, size_t len)
     {
-        size_t pos = input.find_first_of(" \t");
-        if (pos == string::npos)
-            return {input, ""};
-        size_t start = input.find_first_not_of(" \t", pos);
-        if (start == string::npos)
-            return {input.substr(0, pos), ""};
-        return {input.substr(0, pos), input.substr(start)};
+        std::map<string, string> keys;
+        string text;
+        text.reserve(len);
+        for (size_t i = 0; i < len; i++)
+            if (buf[i] != '\0')
+                text.push_back(buf[i]);
+        istringstream lines(text);
+        string line;
+        while (getline(lines, line))
+        {
+            istringstream tok(line);
+            string key, value;
+            if (tok >> key >> value)
+                keys[key] = value;
+        }
+        return keys;
+    }
+    template <class T>
+    static T number(const std::map<string, string> &keys, const char *key, T fallback)
+    {
+        const auto it = keys.find(key);
+        if (it == keys.end())
+            return fallback;
+        istringstream s(it->second);
+        T v;
+        if (!(s >> v))
+            throw std::runtime_error(string("PSRDADA: header value of ") + key + " is not a number: " + it->second);
+        return v;
     }
 };
