@@ -283,7 +283,7 @@ def test_save_simulated_shaped_program_on_the_gpu(eng, tmp_path):
     assert run.returncode == 0, run.stdout + run.stderr
     step, count = map(int, [l for l in run.stdout.splitlines() if l.startswith("dims")][0].split()[1:])
     assert count >= 3
-    x = np.fromfile(tmp_path / "in.u16", np.uint32)
+    x = np.fromfile(out_dir / "in.u16", np.uint32)
     m = eng.MsosmGpuBatch(bw, dms, f0).initialize(0, B, eng.IN_U16, eng.OUT_U16)
     want = np.zeros((count, len(dms), step), np.uint32)
     buf = np.zeros((len(dms), step), np.uint32)
