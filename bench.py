@@ -64,6 +64,11 @@ WORKLOADS = {
     # sorted), which forces F = 2^20; the fused 2-pol fold (msosm_attach_fold_pol2)
     "two_pol_1024": dict(bw=128e6, centre=820e6, n_dms=1024, dm_lo=1.0, dm_hi=1000.0, dm_dist="loguniform",
                          fftpoint=1 << 20, batch=2, nbins=256, samples=1 << 28, period=0.0071, pols=2, sigma=20.0),
+    # DM refinement: 64 simulated sources of 2^20..2^24 samples (log-uniform, seed 5), true
+    # DMs uniform in 10..300, guesses 0.5 DM off, 20 steps each on the smoothed sharpness
+    # (pymsosm.refine); 16 MHz at 1400 MHz, 2 ms period, 2 % Gaussian pulse, -10 dB
+    "refine_64": dict(bw=16e6, centre=1400e6, n_sources=64, len_lo=20, len_hi=24, dm_lo=10.0, dm_hi=300.0,
+                      offset=0.5, period=0.002, duty=0.02, snr_db=-10.0, nbins=256),
 }
 
 
@@ -253,6 +258,9 @@ def cpu_port_rate(w, n_dms_sample: int, substeps: int, seed: int = 3, steps: int
 
 def run_reference(args, w, rank, world):
     if rank != 0:
+        return
+    if "n_sources" in w:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no DM refinement"}))
         return
     n_dms_sample = 32
     substeps = 2
@@ -450,19 +458,21 @@ def run_engine(args, w, rank, world, local):
     import torch
 
     import pymsosm as eng
-    from pymsosm.simulate import pulsar_signal
-
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     bw, f0 = np.float32(w["bw"]), f0_of(w)
     dms = dm_grid(w, rank, world)
     N = w["samples"]
 
-    x = pulsar_signal(N, float(bw), float(f0), w["inject_dm"], w["period"], duty=w["duty"],
-                      snr_db=w["snr_db"], seed=2 + rank)
-    host = torch.from_numpy(x.view(np.float32)).pin_memory()
-    dinp = host.to(dev)
-    del x
+    # the baseband comes from the engine's GPU pulsar simulator (msosm_sim_*)
+    sim = eng.Simulator(bw, f0, np.float32(w["inject_dm"]), np.float32(w["period"]), kind=eng.SIM_GAUSSIAN,
+                        duty=w["duty"], snr_db=w["snr_db"], seed=2 + rank)
+    dc = torch.empty(N, dtype=torch.complex64, device=dev)
+    sim.generate(N, out=dc)
+    torch.cuda.synchronize()
+    del sim
+    dinp = dc.view(torch.float32)
+    host = dinp.cpu().pin_memory()
 
     proc = eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_C64, eng.OUT_NONE)
     proc.set_precision(PRECISIONS[args.precision])
@@ -572,6 +582,67 @@ def run_engine(args, w, rank, world, local):
     print(json.dumps(line))
 
 
+def run_refine(args, w, rank, world, local):
+    """The differentiation workload: every source refined from its guess (20 steps on the
+    smoothed sharpness, two many-DM comb passes per source).  A step of the bench is the
+    refinement of all sources; the metric counts the samples x DM trials the comb passes
+    dedisperse."""
+    import torch
+
+    import pymsosm as eng
+    from pymsosm import refine as R
+
+    torch.cuda.set_device(local)
+    bw, f0 = np.float32(w["bw"]), f0_of(w)
+    rng = np.random.default_rng(5)
+    ns = w["n_sources"]
+    lengths = np.exp2(rng.uniform(w["len_lo"], w["len_hi"], ns)).astype(np.int64)
+    true = rng.uniform(w["dm_lo"], w["dm_hi"], ns)
+    guess = true + np.where(rng.random(ns) < 0.5, -w["offset"], w["offset"])
+    mine = list(range(rank, ns, world))
+    srcs = {}
+    for i in mine:
+        sim = eng.Simulator(bw, f0, np.float32(true[i]), np.float32(w["period"]), kind=eng.SIM_GAUSSIAN,
+                            duty=w["duty"], snr_db=w["snr_db"], seed=1000 + i)
+        srcs[i] = sim.generate(int(lengths[i]))
+    trials = [2 * int(round(st.half_width / st.spacing)) + 1 for st in R.DEFAULT_STAGES]
+
+    def one_pass():
+        return {i: R.refine_dm(srcs[i], bw, f0, guess[i], np.float32(w["period"]), w["nbins"])[0] for i in mine}
+
+    for _ in range(args.warmup):
+        one_pass()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            est = one_pass()
+        torch.cuda.synchronize()
+        t_s = time.perf_counter() - t0
+    barrier(world)
+    t_s = reduce_max(t_s, world)
+    units = reduce_sum(float(sum(int(lengths[i]) for i in mine) * sum(trials) * args.steps), world)
+    err = np.array([est[i] - true[i] for i in mine])
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": units / t_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU pulsar simulator)",
+        "config": {"workload": args.workload, "sources": ns, "samples_per_source": [int(v) for v in lengths],
+                   "comb_trials_per_stage": trials, "gradient_steps": sum(st.steps for st in R.DEFAULT_STAGES),
+                   "bandwidth_hz": float(bw), "f0_hz": float(f0), "period_s": w["period"],
+                   "timing": "host wall clock around whole refinements (planning, simulation excluded)",
+                   "parallelism": f"source-shard x{world}"},
+        "clocks": clk.summary(),
+        "refinement": {"initial_offset_dm": w["offset"], "rms_error_dm": float(np.sqrt(np.mean(err ** 2))),
+                       "max_abs_error_dm": float(np.abs(err).max()),
+                       "within_0p1_dm": int((np.abs(err) < 0.1).sum()), "sources_on_rank0": len(mine)},
+    }
+    print(json.dumps(line))
+
+
 # inverse-transform arithmetic (msosm_set_precision) and the JSON dtype label of each
 PRECISIONS = {"fp32": 0, "bf16x3": 1, "fp16x3": 2}
 DTYPES = {"fp32": "f32", "bf16x3": "bf16x3 (hi/lo operands, f32 accumulate)",
@@ -598,7 +669,7 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     w = dict(WORKLOADS[args.workload])
-    if args.samples:
+    if args.samples and "samples" in w:
         w["samples"] = args.samples
     if args.dm_trials:
         w["n_dms"] = args.dm_trials
@@ -607,6 +678,8 @@ def main():
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, w, rank, world)
+    elif "n_sources" in w:
+        run_refine(args, w, rank, world, local)
     elif w.get("pols", 1) == 2:
         run_two_pol(args, w, rank, world, local)
     else:
