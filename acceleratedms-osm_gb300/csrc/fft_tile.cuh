@@ -5,7 +5,8 @@
 // butterflies per stage with all R inputs in registers.  The default plan takes
 // radix-8 stages (then 4 or 2 to finish); the "big" plan used by the persistent
 // inverse transform takes two register stages of radix 16/32 (N = 512: 16 x 32,
-// N = 1024: 32 x 32, N = 256: 16 x 16, N = 2048: 16 x 8 x 16; see StageRadix).
+// N = 1024: 32 x 32, N = 256: 16 x 16, N = 2048: 16 x 8 x 16, N = 4096: 16 x 16 x 16;
+// see StageRadix).
 // Register DFTs of radix 16 and 32 are composites of radix-8/4/2 kernels with
 // compile-time twiddle constants.  The first stage may read straight from global memory through a
 // loader functor and the last stage may hand its outputs to an epilogue functor
@@ -237,6 +238,7 @@ struct StageRadix
     static constexpr int big = (N == 512)    ? (Ns == 1 ? 16 : 32)
                                : (N == 1024) ? 32
                                : (N == 2048) ? (Ns == 1 ? 16 : (Ns == 16 ? 8 : 16))
+                               : (N == 4096) ? 16
                                : (N == 256)  ? 16
                                : (N == 128)  ? (Ns == 1 ? 8 : 16)
                                              : (rem >= 8 ? 8 : rem);

@@ -39,7 +39,7 @@ using msosm::Twiddles;
 namespace {
 
 constexpr int kMinLog2F = 8;
-constexpr int kMaxLog2F = 22;
+constexpr int kMaxLog2F = 24;
 constexpr size_t kIntermediateBudget = 64ull << 20; // bytes of pass-1 output kept per launch pair
 constexpr unsigned kMaxFusedBins = 8192;
 constexpr int kMaxSlots = 256;                            // intermediate slots of the persistent transform
@@ -549,7 +549,7 @@ extern "C" int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, in
     }
     const long long F = 2ll * M;
     if (!is_pow2(F) || ilog2(F) < kMinLog2F || ilog2(F) > kMaxLog2F)
-        return h->fail(MSOSM_ERR_UNSUPPORTED, "FFT size " + std::to_string(F) + " outside [2^8, 2^22]");
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "FFT size " + std::to_string(F) + " outside [2^8, 2^24]");
     h->M = M;
     h->F = (int)F;
     h->B = batch;

@@ -12,7 +12,7 @@ namespace msosm {
 template <int N>
 struct TileCfg
 {
-    static constexpr int COLS = (N <= 512) ? 16 : (N == 1024 ? 8 : 4);
+    static constexpr int COLS = (N <= 512) ? 16 : 8192 / N; // 8192-point tiles from N = 512 up
     static constexpr int POINTS = N * COLS;
     static constexpr int THREADS = (POINTS / 16 < 32) ? 32 : (POINTS / 16);
     static constexpr int SMEM_DATA = TileGeom<N, COLS>::SMEM_ELEMS; // float2 elements

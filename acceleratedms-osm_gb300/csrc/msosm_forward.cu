@@ -155,6 +155,7 @@ static cudaError_t fwd_pass1_dispatch(const Geom &g, const Twiddles &tw, const v
     case 512: return fwd_pass1<512, FMT>(g, tw, in, tail, tail_next, T, B, st);
     case 1024: return fwd_pass1<1024, FMT>(g, tw, in, tail, tail_next, T, B, st);
     case 2048: return fwd_pass1<2048, FMT>(g, tw, in, tail, tail_next, T, B, st);
+    case 4096: return fwd_pass1<4096, FMT>(g, tw, in, tail, tail_next, T, B, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -172,6 +173,7 @@ static cudaError_t fwd_pass2_dispatch(const Geom &g, const Twiddles &tw, const f
     case 512: return fwd_pass2<512>(g, tw, T, ring, rbi, B, st);
     case 1024: return fwd_pass2<1024>(g, tw, T, ring, rbi, B, st);
     case 2048: return fwd_pass2<2048>(g, tw, T, ring, rbi, B, st);
+    case 4096: return fwd_pass2<4096>(g, tw, T, ring, rbi, B, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -1004,10 +1004,27 @@ cudaError_t persist_mode(const PersistArgs &a, int sms, cudaStream_t st, Persist
     }
 }
 
+// The largest transforms (F = 2^23, 2^24: the plain overlap-save processor at long
+// smears) only with the series / fold outputs a single-DM processor uses.
+template <int N1, int N2>
+cudaError_t persist_mode_large(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
+{
+    switch (a.out_mode)
+    {
+    case OUT_C64: return persist_launch<N1, N2, OUT_C64>(a, sms, st, plan);
+    case OUT_U16: return persist_launch<N1, N2, OUT_U16>(a, sms, st, plan);
+    case OUT_FOLD: return persist_launch<N1, N2, OUT_FOLD>(a, sms, st, plan);
+    case OUT_C64 | OUT_FOLD: return persist_launch<N1, N2, OUT_C64 | OUT_FOLD>(a, sms, st, plan);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t persist_dispatch(int L, const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
 {
     switch (L)
     {
+    case 23: return persist_mode_large<2048, 4096>(a, sms, st, plan);
+    case 24: return persist_mode_large<4096, 4096>(a, sms, st, plan);
     case 16: return persist_mode<256, 256>(a, sms, st, plan);
     case 17: return persist_mode<256, 512>(a, sms, st, plan);
     case 18: return persist_mode<512, 512>(a, sms, st, plan);
@@ -1065,7 +1082,7 @@ cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned lon
     return e;
 }
 
-bool persist_supported(int L) { return L >= 16 && L <= 22; }
+bool persist_supported(int L) { return L >= 16 && L <= 24; }
 
 cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan)
 {

@@ -374,9 +374,9 @@ static int sim_setup(msosm_sim_t *s)
     int M = 1 << 15;
     while ((unsigned long long)M < s->nd + 1)
         M <<= 1;
-    if (2ll * M > (1ll << 22))
-        return s->fail(MSOSM_ERR_UNSUPPORTED, "dispersion smear above 2^21 samples (Nd = " + std::to_string(s->nd) +
-                                                  "): the filter transform would exceed 2^22 points");
+    if (2ll * M > (1ll << 24))
+        return s->fail(MSOSM_ERR_UNSUPPORTED, "dispersion smear of 2^23 samples or more (Nd = " + std::to_string(s->nd) +
+                                                  "): the filter transform would exceed 2^24 points");
     const int B = (int)std::max<unsigned long long>(1, kChunkTarget / (unsigned long long)M);
     int rc = msosm_filter_create(s->bw, s->f0, M, &s->filt);
     if (rc != MSOSM_OK)

@@ -16,7 +16,7 @@
 // Differences a caller can see: the random sequences differ from the reference's
 // mt19937 / default_random_engine draws (same distributions); no simulated_*.bin /
 // random_reference.bin cache files are read or written; dispersion smear is limited
-// to Nd < 2^21 samples.  As in the reference, the buffers live until the process
+// to Nd < 2^23 samples.  As in the reference, the buffers live until the process
 // exits (its destructor frees nothing), so they may stay registered with CUDA.
 #pragma once
 #include "AWGN.h"

@@ -78,7 +78,9 @@ int osm_plan(float bw, float dm, float f0, unsigned long *nd_out, unsigned long 
  *   bool fold) (msosm_gpu_batch.h:19, msosm_gpu_batch.cpp:12-151): fftpoint 0
  *   picks 2*M_min, otherwise M = max(fftpoint/2, M_min).  in_format is an
  *   MSOSM_IN_* value, out_mode an MSOSM_OUT_* mask.  batch need not be a
- *   multiple of 4.  fftpoint must come out a power of two in [256, 2^22].
+ *   multiple of 4.  fftpoint must come out a power of two in [256, 2^24]; 2^23 and 2^24
+ *   (long plain overlap-save filters) support MSOSM_OUT_C64 or MSOSM_OUT_U16 series
+ *   output and the fused fold.
  */
 int msosm_create(float bw, float f0, const float *dms, int num_dms, msosm_t **out);
 int msosm_init(msosm_t *h, int fftpoint, int batch, int in_format, int out_mode);
@@ -329,7 +331,7 @@ int msosm_set_response(msosm_t *h, int dm_index, const float *H);
  * msosm_awgn           AWGN::generateNoiseSamples: n complex samples (2n floats, host or
  *                      device) with independent N(mean, stddev^2) quadratures, samples
  *                      first .. first+n-1 of the seed's noise stream.
- * Dispersion smear is limited to Nd < 2^21 samples (filter transform <= 2^22 points). */
+ * Dispersion smear is limited to Nd < 2^23 samples (filter transform <= 2^24 points). */
 #define MSOSM_SIM_TEST_PULSE 0
 #define MSOSM_SIM_GAUSSIAN 1
 #define MSOSM_SIM_IMPULSES 2

@@ -223,6 +223,29 @@ def test_osm_matches_oracle(eng, orc, golden_osm):
     assert _compare_stream(got, ref, 1) < TOL
 
 
+def test_osm_at_the_largest_transform(eng, orc):
+    """Plain overlap-save at the many-DM grid's top end: 64 MHz at 1368 MHz, DM 200,
+    Nd = 2.48e6, so Prepare_OSM's order gives F = 2^24 (osm_prepare.cpp:17-30); the
+    series against the FP64 oracle after the first window, and DM 0 as the identity."""
+    bw, f0 = np.float32(64e6), np.float32(1368e6)
+    m = eng.OsmGpuBatch(bw, np.float32(200.0), f0).initialize(0, 1, eng.IN_C64, eng.OUT_C64)
+    assert m.fftpoint == 1 << 24 and m.nd[0] == orc.osm_nd(bw, np.float32(200.0), f0)
+    plan = orc.Plan(bw, f0, [200.0], m.fftpoint, batch=1)
+    plan.delays[:] = 0
+    plan.delaycount = 1
+    rng = np.random.default_rng(24)
+    chunks = [(rng.standard_normal(m.M) + 1j * rng.standard_normal(m.M)).astype(np.complex64) for _ in range(3)]
+    got = _run_engine(m, chunks)
+    ref = _run_oracle(orc, plan, 1, chunks)
+    err = _compare_stream(got, ref, 1)
+    print(f"OSM F = 2^24, DM 200: rel-L2 vs FP64 oracle {err:.2e}")
+    assert err < TOL
+    ident = eng.OsmGpuBatch(bw, np.float32(0.0), f0).initialize(1 << 24, 1, eng.IN_C64, eng.OUT_C64)
+    out = _run_engine(ident, chunks)
+    for c, o in zip(chunks, out):
+        assert rel_l2(o.reshape(-1), c) < 1e-6
+
+
 def test_c1_single_dm_full_size(eng, orc):
     """Single-DM workload at full size: 16 MHz at 1400 MHz, DM 50, 2^22 complex64
     samples of a dispersed pulsar (period 33 ms, 5 % duty, -10 dB), F = 2^16,
