@@ -834,6 +834,14 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         (e = msosm::tc_absmax(h->d_ring + (size_t)rbi * h->F, (size_t)h->B * h->F, h->d_absmax, st)) != cudaSuccess)
         return h->cuda_fail(e, "spectra bound launch");
 
+    // a step with nothing to produce (no series output, no fold) only advances the
+    // stream: the tail and the ring of spectra, e.g. to skip the ring's warm-up
+    if (h->out_mode == MSOSM_OUT_NONE && !h->fold && !h->pair_out)
+    {
+        h->tail_cur ^= 1;
+        h->step++;
+        return MSOSM_OK;
+    }
     msosm::InvArgs a{};
     a.ring = h->d_ring;
     a.H = h->d_H;
@@ -978,8 +986,6 @@ extern "C" int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *
         return h->fail(MSOSM_ERR_STATE, "msosm_process before msosm_init");
     if (!in || nsteps < 0)
         return h->fail(MSOSM_ERR_ARG, "null input");
-    if (h->out_mode == MSOSM_OUT_NONE && !h->fold && !h->pair_out)
-        return h->fail(MSOSM_ERR_STATE, "no output mode and no fold attached");
     cudaStream_t st = (cudaStream_t)stream;
     // device input is read in place only when aligned to its element size (the
     // kernels use 8/4/2-byte vector loads); anything else goes through staging

@@ -128,7 +128,9 @@ int msosm_get_response(const msosm_t *h, int dm_index, float *out);
  * pageable host `in` may be reused on return.  Host inputs are copied on the
  * handle's own stream, overlapping the previous step's transforms.  Replaces
  * MSOSM_GPU_BATCH::filter_block_uint16(uint16_pair*) (msosm_gpu_batch.h:20,
- * msosm_gpu_batch.cpp:178-236) and its complex64 / int8 variants. */
+ * msosm_gpu_batch.cpp:178-236) and its complex64 / int8 variants.  A handle with
+ * MSOSM_OUT_NONE and no fold attached runs only the forward transform: the step
+ * advances the stream (tail, ring of spectra) and produces nothing. */
 int msosm_process(msosm_t *h, const void *in, void *stream);
 /* `nsteps` consecutive steps from one contiguous input of nsteps*B*M samples. */
 int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *stream);
