@@ -224,6 +224,23 @@ def reduce_sum(x: float, world: int) -> float:
     return float(t.item())
 
 
+def gather_profiles(folded: np.ndarray, world: int) -> np.ndarray:
+    """The per-rank [D][K] folded profiles of an interleaved DM share (dm_grid), gathered
+    on the host into the whole grid's [D * world][K] in grid order (row i from rank
+    i % world).  Every rank gets the result; this is the only exchange of the sharded
+    path, after the timed region."""
+    if world <= 1:
+        return folded
+    import torch.distributed as dist
+
+    parts = [None] * world
+    dist.all_gather_object(parts, np.ascontiguousarray(folded))
+    full = np.empty((sum(p.shape[0] for p in parts), folded.shape[1]), folded.dtype)
+    for r, p in enumerate(parts):
+        full[r::world] = p
+    return full
+
+
 # ----------------------------------------------------------------------------
 def cpu_port_rate(w, n_dms_sample: int, substeps: int, seed: int = 3, steps: int = 1, warmup: int = 0):
     """FP32 CPU port (oracle/) on a bounded sample: returns (rate, seconds, description)."""
@@ -554,10 +571,14 @@ def run_engine(args, w, rank, world, local):
         mad = np.median(np.abs(p - base)) * 1.4826
         return float((p.max() - base) / mad) if mad > 0 else 0.0
 
-    s = np.array([snr(p) for p in folded_host])
+    # the whole grid's profiles on every rank (host gather of the DM shards)
+    all_folded = gather_profiles(folded_host, world)
+    all_dms = dm_grid(w, 0, 1) if world == 1 else np.sort(np.concatenate(
+        [dm_grid(w, r, world) for r in range(world)]))
+    s = np.array([snr(p) for p in all_folded])
     best = int(np.argmax(s))
-    check = {"best_dm": float(dms[best]), "snr_best": float(s[best]), "snr_dm_lowest": float(s[0]),
-             "injected_dm": w["inject_dm"]}
+    check = {"best_dm": float(all_dms[best]), "snr_best": float(s[best]), "snr_dm_lowest": float(s[0]),
+             "injected_dm": w["inject_dm"], "dm_trials_gathered": int(len(all_folded))}
 
     if rank != 0:
         return

@@ -1,8 +1,9 @@
 """Multi-rank host logic of bench.py on CPU (gloo, world size 2).
 
 DM trials shard across ranks with no data-path collective: each rank takes an
-interleaved share of a 512*N-trial grid (equal work per rank, weak scaling), and
-the timing is the maximum over ranks.  Only one GPU exists in this run, so this
+interleaved share of a 512*N-trial grid (equal work per rank, weak scaling), the
+timing is the maximum over ranks, and the folded profiles are gathered on the host
+afterwards.  Only one GPU exists in this run, so this
 is the coverage of the N > 1 path.
 """
 from __future__ import annotations
@@ -29,8 +30,11 @@ def _worker(rank, world, port, q):
     grid = bench.dm_grid(wl, r, w)
     t = bench.reduce_max(float(10 + rank), w)
     s = bench.reduce_sum(float(len(grid)), w)
+    # the host gather of the per-rank [D][K] profiles puts row i of the grid at i
+    prof = np.stack([np.full(4, float(d)) for d in grid])
+    full = bench.gather_profiles(prof, w)
     bench.barrier(w)
-    q.put((r, grid.tolist(), t, s))
+    q.put((r, grid.tolist(), t, s, full[:, 0].tolist()))
     import torch.distributed as dist
 
     dist.destroy_process_group()
@@ -56,6 +60,8 @@ def test_dm_sharding_and_reductions():
     assert len(full) == 1024 and full[0] == 0.0 and abs(full[-1] - 200.0) < 1e-4
     assert all(o[2] == 11.0 for o in out)  # max over ranks
     assert all(o[3] == 1024.0 for o in out)  # total trials
+    for o in out:  # every rank holds the whole grid's profiles, in grid order
+        np.testing.assert_array_equal(np.array(o[4], np.float32), full)
 
 
 def test_single_rank_grid_is_the_workload():
