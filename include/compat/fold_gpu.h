@@ -52,6 +52,8 @@ class Fold_GPU
         for (unsigned long i = 0; i < time_bin; i++)
             outfile << folded_data[i] << endl;
     }
+    // the engine's fold handle, for callers that mix the class with the C ABI
+    msosm_fold_t *handle() { return f; }
 
   public:
     float *folded_data = nullptr;

@@ -298,3 +298,104 @@ def test_save_simulated_shaped_program_on_the_gpu(eng, tmp_path):
         got = np.fromfile(p, np.uint32)
         assert got.size == count * step
         assert np.array_equal(got, want[:, d, :].reshape(-1)), p.name
+
+
+DADA_PROGRAM = r"""
+#include "globals.h"
+#include "msosm_gpu_batch.h"
+#include "fold_gpu.h"
+#include "psrdada.h"
+#include <cstdio>
+#include <vector>
+
+// argv: dada file, dm, batch, period, bins.  The msosm_psrdada.cpp flow: the reader's
+// header gives the band; two polarisations dedispersed, 2-pol intensity folded.  NBIT 16
+// runs the reference's classes; NBIT 8 the C ABI's int8 input on the same engine.
+int main(int argc, char **argv)
+{
+    if (argc != 6)
+        return 2;
+    float dm = atof(argv[2]);
+    const int batch = atoi(argv[3]);
+    const float period = atof(argv[4]);
+    const unsigned long bins = strtoul(argv[5], nullptr, 10);
+    PSRDADA f(argv[1]);
+    const float bw = f.bw * 1e6f, f0 = (f.fc - f.bw / 2) * 1e6f;
+    msosm_t *h[2];
+    for (int p = 0; p < 2; p++)
+    {
+        msosm_compat::check(msosm_create(bw, f0, &dm, 1, &h[p]), nullptr, "create");
+        msosm_compat::check(msosm_init(h[p], 0, batch, f.nbit == 8 ? MSOSM_IN_I8 : MSOSM_IN_U16, MSOSM_OUT_C64), h[p],
+                            "init");
+    }
+    int M = 0;
+    msosm_get_dims(h[0], &M, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    const unsigned long n = (unsigned long)batch * M;
+    Fold_GPU fold(period, bw, n, "fold_dada.txt", bins);
+    f.initBuffer(n);
+    printf("M %d reads %lu\n", M, f.readCount);
+    for (unsigned long r = 0; r < f.readCount; r++)
+    {
+        if (!f.readSamples())
+            return 3;
+        const void *p1 = f.nbit == 8 ? (const void *)f.pol1_i8 : (const void *)f.pol1_in;
+        const void *p2 = f.nbit == 8 ? (const void *)f.pol2_i8 : (const void *)f.pol2_in;
+        msosm_compat::check(msosm_process(h[0], p1, nullptr), h[0], "process");
+        msosm_compat::check(msosm_process(h[1], p2, nullptr), h[1], "process");
+        msosm_compat::check(msosm_fold_accumulate(fold.handle(), msosm_device_output(h[0]), msosm_device_output(h[1]),
+                                                  nullptr), nullptr, "fold");
+    }
+    msosm_sync(h[0], nullptr);
+    fold.get_folded_data();
+    for (unsigned long k = 0; k < fold.time_bin; k++)
+        printf("%.9g\n", fold.folded_data[k]);
+    msosm_destroy(h[0]);
+    msosm_destroy(h[1]);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("nbit", [16, 8])
+def test_psrdada_file_through_the_engine(eng, orc, tmp_path, nbit):
+    exe = _compile(tmp_path, "dada_prog", DADA_PROGRAM)
+    bw_mhz, fc_mhz, dm, B, period, K = 16.0, 1008.0, 5.0, 8, 0.0041, 64
+    bw, f0 = np.float32(bw_mhz * 1e6), np.float32((fc_mhz - bw_mhz / 2) * 1e6)
+    m = eng.MsosmGpuBatch(bw, [dm], f0).initialize(0, B, eng.IN_C64, eng.OUT_C64)
+    n = B * m.M
+    reads = 3
+    rng = np.random.default_rng(nbit)
+    pols = []
+    for _ in range(2):
+        iq = np.clip(np.round(rng.normal(0, 20, (reads * n, 2))), -127, 127).astype(np.int64)
+        pols.append(iq)
+    # body: frames of 2048 samples, pol 1 frame k then pol 2 frame k
+    frames = reads * n // 2048
+    if nbit == 16:
+        words = [((p[:, 0] + 32768) | ((p[:, 1] + 32768) << 16)).astype(np.uint32) for p in pols]
+        body = np.stack([w.reshape(frames, 2048) for w in words], axis=1).reshape(-1).tobytes()
+    else:
+        b8 = [p.astype(np.int8).reshape(frames, 2048 * 2) for p in pols]
+        body = np.stack(b8, axis=1).reshape(-1).tobytes()
+    hdr = (f"HDR_VERSION 1.0\nBW {bw_mhz}\nFREQ {fc_mhz}\nNBIT {nbit}\nNCHAN 1\nNDIM 2\nNPOL 2\n").encode()
+    f = tmp_path / f"obs{nbit}.dada"
+    f.write_bytes(hdr + b"\0" * (4096 - len(hdr)) + body)
+    run = subprocess.run([str(exe), str(f), str(dm), str(B), str(period), str(K)], capture_output=True, text=True,
+                         cwd=tmp_path, timeout=600)
+    assert run.returncode == 0, run.stdout + run.stderr
+    lines = run.stdout.splitlines()
+    assert lines[0] == f"M {m.M} reads {reads}"
+    got = np.array([float(v) for v in lines[1:]])
+
+    plan = orc.Plan(bw, f0, [dm], 0, batch=B)
+    oms = [orc.Msosm(plan, B, fp64=True) for _ in range(2)]
+    s_ = np.zeros(K)
+    c_ = np.zeros(K, np.uint64)
+    dt = 1.0 / float(bw)
+    for r in range(reads):
+        xs = [(p[r * n:(r + 1) * n, 0] + 1j * p[r * n:(r + 1) * n, 1]).astype(np.complex64) for p in pols]
+        ya = oms[0].process(xs[0])[0].reshape(-1)
+        yb = oms[1].process(xs[1])[0].reshape(-1)
+        orc.fold(orc.intensity2(ya, yb), K, r * n * dt, dt, float(np.float32(period)), s_, c_)
+    ref = orc.fold_finalize(s_, c_)
+    assert rel_l2(got, ref) < 1e-4
