@@ -279,6 +279,11 @@ struct msosm_s
     int cuda_fail(cudaError_t e, const char *what)
     {
         err = std::string(what) + ": " + cudaGetErrorString(e);
+        const char *detail = msosm::launch_failure_detail();
+        if (detail && *detail)
+            err += std::string(" [") + detail + "]";
+        msosm::set_launch_failure_detail("", "", 0, 0, 0, 0);
+        (void)cudaGetLastError(); // a non-sticky error must not surface in a later call
         return MSOSM_ERR_CUDA;
     }
     void release()

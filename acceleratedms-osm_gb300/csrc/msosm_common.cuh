@@ -123,6 +123,8 @@ inline cudaError_t ensure_smem(KERNEL k, size_t bytes, size_t (&granted)[kMaxDev
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess)
         granted[dev] = bytes;
+    else
+        (void)cudaGetLastError(); // reported through the return value, not left for later calls
     return e;
 }
 

@@ -11,7 +11,27 @@
 //           straight into spectra-ring slot rbi + b.
 #include "msosm_common.cuh"
 
+#include <cstdio>
+
 namespace msosm {
+
+namespace {
+thread_local char g_launch_detail[192] = "";
+}
+
+const char *launch_failure_detail() { return g_launch_detail; }
+
+void set_launch_failure_detail(const char *kernel, const char *step, unsigned gx, unsigned gy, unsigned block,
+                               size_t smem)
+{
+    if (!kernel || !*kernel)
+    {
+        g_launch_detail[0] = '\0'; // cleared
+        return;
+    }
+    std::snprintf(g_launch_detail, sizeof g_launch_detail, "%s: %s (grid %u x %u, %u threads, %zu bytes shared)",
+                  kernel, step, gx, gy, block, smem);
+}
 
 template <int FMT>
 struct FwdLoader
@@ -117,13 +137,19 @@ static cudaError_t fwd_pass1(const Geom &g, const Twiddles &tw, const void *in, 
     using C = TileCfg<N>;
     auto k = fwd_pass1_kernel<N, FMT>;
     static size_t granted[kMaxDevices] = {};
+    dim3 grid(g.N1 / C::COLS, B);
     cudaError_t e = ensure_smem(k, C::SMEM_BYTES, granted);
     if (e != cudaSuccess)
+    {
+        set_launch_failure_detail("fwd_pass1", "shared-memory attribute", grid.x, grid.y, C::THREADS, C::SMEM_BYTES);
         return e;
-    dim3 grid(g.N1 / C::COLS, B);
+    }
     k<<<grid, C::THREADS, C::SMEM_BYTES, st>>>(in, tail, tail_next, T, tw.twN2, tw.lo, tw.hi, B, g.M, g.N1,
                                                   __builtin_ctz((unsigned)g.N2));
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        set_launch_failure_detail("fwd_pass1", "launch", grid.x, grid.y, C::THREADS, C::SMEM_BYTES);
+    return e;
 }
 
 template <int N>
@@ -133,12 +159,18 @@ static cudaError_t fwd_pass2(const Geom &g, const Twiddles &tw, const float2 *T,
     using C = TileCfg<N>;
     auto k = fwd_pass2_kernel<N>;
     static size_t granted[kMaxDevices] = {};
+    dim3 grid(g.N2 / C::COLS, B);
     cudaError_t e = ensure_smem(k, C::SMEM_BYTES, granted);
     if (e != cudaSuccess)
+    {
+        set_launch_failure_detail("fwd_pass2", "shared-memory attribute", grid.x, grid.y, C::THREADS, C::SMEM_BYTES);
         return e;
-    dim3 grid(g.N2 / C::COLS, B);
+    }
     k<<<grid, C::THREADS, C::SMEM_BYTES, st>>>(T, ring, tw.twN1, rbi, g.M, g.N2);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        set_launch_failure_detail("fwd_pass2", "launch", grid.x, grid.y, C::THREADS, C::SMEM_BYTES);
+    return e;
 }
 
 template <int FMT>
@@ -156,7 +188,7 @@ static cudaError_t fwd_pass1_dispatch(const Geom &g, const Twiddles &tw, const v
     case 1024: return fwd_pass1<1024, FMT>(g, tw, in, tail, tail_next, T, B, st);
     case 2048: return fwd_pass1<2048, FMT>(g, tw, in, tail, tail_next, T, B, st);
     case 4096: return fwd_pass1<4096, FMT>(g, tw, in, tail, tail_next, T, B, st);
-    default: return cudaErrorInvalidValue;
+    default: set_launch_failure_detail("fwd_pass1", "no tile for this size", g.N2, 0, 0, 0); return cudaErrorInvalidValue;
     }
 }
 
@@ -174,7 +206,7 @@ static cudaError_t fwd_pass2_dispatch(const Geom &g, const Twiddles &tw, const f
     case 1024: return fwd_pass2<1024>(g, tw, T, ring, rbi, B, st);
     case 2048: return fwd_pass2<2048>(g, tw, T, ring, rbi, B, st);
     case 4096: return fwd_pass2<4096>(g, tw, T, ring, rbi, B, st);
-    default: return cudaErrorInvalidValue;
+    default: set_launch_failure_detail("fwd_pass2", "no tile for this size", g.N1, 0, 0, 0); return cudaErrorInvalidValue;
     }
 }
 

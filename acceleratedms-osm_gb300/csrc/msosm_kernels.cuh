@@ -48,6 +48,12 @@ struct FoldArgs
 
 // Forward: B overlapping windows of the [tail | new input] stream -> spectra ring slots.
 // Pass 1 (decode + column transforms -> T), pass 2 (row transforms -> ring slot rbi+b).
+// Which step of the last failed launch helper on this thread went wrong (the shared-
+// memory attribute or the launch itself, with the launch geometry); empty if none.
+const char *launch_failure_detail();
+void set_launch_failure_detail(const char *kernel, const char *step, unsigned gx, unsigned gy, unsigned block,
+                               size_t smem);
+
 cudaError_t launch_forward_p1(const Geom &g, const Twiddles &tw, int in_format, const void *in, const float2 *tail,
                               float2 *tail_next, float2 *T, int B, cudaStream_t st);
 cudaError_t launch_forward_p2(const Geom &g, const Twiddles &tw, const float2 *T, float2 *ring, int rbi, int B,

@@ -877,9 +877,16 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
 {
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
+    {
+        set_launch_failure_detail("persistent inverse transform", "shared-memory attribute", 0, 0, P_THREADS, smem);
         return e;
+    }
     if (carveout_blocks > 0 && (e = prefer_carveout(k, smem, carveout_blocks)) != cudaSuccess)
+    {
+        (void)cudaGetLastError();
+        set_launch_failure_detail("persistent inverse transform", "carveout attribute", 0, 0, P_THREADS, smem);
         return e;
+    }
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P_THREADS, smem);
     if (e != cudaSuccess)
@@ -928,7 +935,11 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, k, a, extra...);
-    return e != cudaSuccess ? e : cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    if (e != cudaSuccess)
+        set_launch_failure_detail("persistent inverse transform", "launch", grid, 1, P_THREADS, smem);
+    return e;
 }
 
 template <int N1, int N2, int MODE>
