@@ -925,15 +925,27 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
     cfg.blockDim = dim3(P_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
+    // the window cannot exceed the device's maximum access-policy window (the largest
+    // transforms' slot rings do): it then covers the first part of the ring
+    static int max_window[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        dev = 0;
+    if (max_window[dev] == 0 &&
+        cudaDeviceGetAttribute(&max_window[dev], cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess)
+    {
+        (void)cudaGetLastError();
+        max_window[dev] = -1;
+    }
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
     attr[0].val.accessPolicyWindow.base_ptr = (void *)a.T;
-    attr[0].val.accessPolicyWindow.num_bytes = slot_bytes;
+    attr[0].val.accessPolicyWindow.num_bytes = std::min(slot_bytes, (size_t)std::max(max_window[dev], 0));
     attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
     attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
     attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = max_window[dev] > 0 ? 1 : 0;
     e = cudaLaunchKernelEx(&cfg, k, a, extra...);
     if (e == cudaSuccess)
         e = cudaGetLastError();

@@ -127,3 +127,72 @@ def test_fused_two_pol_fold_rejects_series_output(eng):
     fold = eng.FoldGpu(np.float32(0.0031), bw, 4 * a.M, 64, len(dms))
     with pytest.raises(eng.MsosmError):
         a.attach_fold_pol2(b, fold)
+
+
+def test_two_pol_int8_full_size(eng, orc):
+    """The batching configuration at full size: 2 x 2^28 int8 samples, all 1024
+    log-uniform DMs, F = 2^20.  The fused 2-pol fold (no series) of every trial against
+    the reference-shaped path (series out, then the 2-pol fold); the series of 16 trials
+    spread over the grid (the widest, delaycount 477, included) against the FP64 oracle
+    over the last 16 windows of the 512, all past every trial's ring warm-up."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(4)
+    dms = np.sort(np.exp(rng.uniform(np.log(1.0), np.log(1000.0), 1024))).astype(np.float32)
+    bw, f0 = np.float32(128e6), np.float32(756e6)
+    B, N, K, period = 2, 1 << 28, 256, np.float32(0.0071)
+    dev = torch.device("cuda")
+    pols = []
+    for p in range(2):
+        g = torch.empty(N, dtype=torch.complex64, device=dev)
+        eng.awgn(N, 0.0, 20.0, seed=40 + p, out=g)
+        iq = torch.view_as_real(g).reshape(-1).round().clamp(-127, 127).to(torch.int8)
+        del g
+        pols.append(iq)
+    torch.cuda.synchronize()
+    fus = [eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 20, B, eng.IN_I8, eng.OUT_NONE) for _ in range(2)]
+    ref = [eng.MsosmGpuBatch(bw, dms, f0).initialize(1 << 20, B, eng.IN_I8, eng.OUT_C64) for _ in range(2)]
+    assert fus[0].M == 1 << 19 and fus[0].delaycount == 477
+    step = B * fus[0].M
+    fold_fus = eng.FoldGpu(period, bw, step, K, len(dms))
+    fold_ref = eng.FoldGpu(period, bw, step, K, len(dms))
+    fus[0].attach_fold_pol2(fus[1], fold_fus)
+    pick = np.unique(np.r_[np.linspace(0, len(dms) - 1, 16).round().astype(int), len(dms) - 1])
+    ser = [eng.MsosmGpuBatch(bw, dms[pick], f0).initialize(1 << 20, B, eng.IN_I8, eng.OUT_C64) for _ in range(2)]
+    steps = N // step
+    tail = 8  # the last 8 steps (16 windows) are compared, all past every trial's warm-up
+    got = [np.zeros((len(pick), tail * step), np.complex64) for _ in range(2)]
+    for s in range(steps):
+        for p in range(2):
+            src = pols[p][2 * s * step:2 * (s + 1) * step]
+            fus[p].filter_block(src)
+            ref[p].filter_block(src)
+            ser[p].filter_block(src)
+        fold_ref.accumulate(ref[0].get_output_pointer(), ref[1].get_output_pointer())
+        if s >= steps - tail:
+            for p in range(2):
+                o = np.zeros((len(pick), B, ser[p].M), np.complex64)
+                ser[p].get_output(o)
+                ser[p].synchronize()
+                j = s - (steps - tail)
+                got[p][:, j * step:(j + 1) * step] = o.reshape(len(pick), -1)
+    fus[1].synchronize()
+    _, fsums, fcnts = fold_fus.read()
+    _, rsums, rcnts = fold_ref.read()
+    # every trial: the fused fold folds what the reference-shaped path folds
+    assert np.abs(fcnts.astype(np.int64) - rcnts.astype(np.int64)).max() <= 2
+    for d in range(len(dms)):
+        assert rel_l2(fsums[d], rsums[d]) < 1e-5, d
+    # the picked trials' series against the FP64 oracle after each trial's warm-up
+    host = [pols[p].cpu().numpy() for p in range(2)]
+    plan = orc.Plan(bw, f0, dms[pick], 1 << 20, batch=B)
+    assert (steps - tail) * B > plan.delaycount + 2  # every compared window is past the warm-up
+    for p in range(2):
+        om = orc.Msosm(plan, B, fp64=True)
+        r = np.zeros((len(pick), tail * step), np.complex128)
+        for s in range(steps):
+            o = om.process(orc.decode_i8(host[p][2 * s * step:2 * (s + 1) * step]), want_output=s >= steps - tail)
+            if o is not None:
+                j = s - (steps - tail)
+                r[:, j * step:(j + 1) * step] = o.reshape(len(pick), -1)
+        for k in range(len(pick)):
+            assert rel_l2(got[p][k], r[k]) < 1e-4, (p, k, float(dms[pick[k]]))
