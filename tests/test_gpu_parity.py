@@ -169,10 +169,13 @@ def test_fused_fold_matches_oracle(eng, orc):
             inten = orc.intensity1(o[d].reshape(-1).astype(np.complex64))
             orc.fold(inten, K, t0, dt, float(period), s, c_)
             t0 += n * dt
-        assert int(cnts[d].sum()) == int(c_.sum())
-        assert np.abs(cnts[d].astype(np.int64) - c_.astype(np.int64)).sum() <= 2
-        assert rel_l2(sums[d], s) < TOL
+        moved = int(np.abs(cnts[d].astype(np.int64) - c_.astype(np.int64)).sum())
         prof = orc.fold_finalize(s, c_)
+        print(f"fused fold vs FP64 foldDataPhase, trial {d}: {moved} sample(s) in another bin of "
+              f"{int(c_.sum())}, sums rel-L2 {rel_l2(sums[d], s):.2e}, profile rel-L2 {rel_l2(folded[d], prof):.2e}")
+        assert int(cnts[d].sum()) == int(c_.sum())
+        assert moved <= 2
+        assert rel_l2(sums[d], s) < TOL
         assert rel_l2(folded[d], prof) < TOL
         assert int(np.argmax(folded[d])) == int(np.argmax(prof))
 
