@@ -266,6 +266,7 @@ struct msosm_s
     void *d_tc_op = nullptr;
     unsigned *d_absmax = nullptr;
     float hmax = 1.0f;
+    uint64_t *graph_phase = nullptr; // while capturing a graph: the fold's device-resident phase
     float *pair_out = nullptr;      // first polarisation of a 2-pol fused fold: |a|^2 goes here
     const float *pair_in = nullptr; // second polarisation: folds sqrt(pair_in + |b|^2)
     Profiler prof;
@@ -866,6 +867,7 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
     {
         a.out_mode |= msosm::OUT_FOLD;
         a.fold = h->fold->args();
+        a.fold.phase_dev = h->graph_phase;
         if (h->pair_in)
             a.out_mode |= msosm::OUT_PAIR;
     }
@@ -932,6 +934,10 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         if (e != cudaSuccess)
             return h->cuda_fail(e, "inverse transform launch (pass 2)");
     }
+    if (h->fold && h->graph_phase &&
+        (e = msosm::launch_phase_advance(h->graph_phase, (uint64_t)((uint64_t)h->B * (uint64_t)h->M) * a.fold.dphase,
+                                         st)) != cudaSuccess)
+        return h->cuda_fail(e, "fold phase advance");
     if (h->fold)
         h->fold->t_start += (double)((size_t)h->B * h->M) * h->fold->dt; // fold_gpu.cpp:53
     if (h->writer)
@@ -976,6 +982,129 @@ extern "C" int msosm_writer_copy_output(msosm_writer_t *w, msosm_t *h, void *str
     std::string werr;
     const int rc = msosm::writer_submit_device(w, h->d_out_u16, (cudaStream_t)stream, werr);
     return rc == MSOSM_OK ? rc : h->fail(rc, werr);
+}
+
+// ---- CUDA-graph capture of consecutive steps ------------------------------------
+struct msosm_graph_s
+{
+    msosm_t *h = nullptr;
+    int nsteps = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t *d_phase = nullptr; // the fold's phase, read and advanced by the graph's calls
+    ~msosm_graph_s()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        dfree(d_phase);
+    }
+};
+
+static long long gcd_ll(long long a, long long b) { return b ? gcd_ll(b, a % b) : a; }
+
+extern "C" int msosm_graph_create(msosm_t *h, const void *in, int nsteps, msosm_graph_t **out)
+{
+    if (!h || !out)
+        return MSOSM_ERR_ARG;
+    *out = nullptr;
+    if (!h->inited)
+        return h->fail(MSOSM_ERR_STATE, "graph_create before init");
+    if (!h->persist)
+        return h->fail(MSOSM_ERR_UNSUPPORTED, "graph capture needs the persistent transform (fftpoint >= 65536)");
+    if (h->writer || h->prof.on)
+        return h->fail(MSOSM_ERR_STATE, "graph capture with a writer attached or timing on");
+    if (!in || !is_device_pointer(in) || ((uintptr_t)in % in_elem_bytes(h->in_format)) != 0)
+        return h->fail(MSOSM_ERR_ARG, "graph input must be aligned device memory");
+    // the ring slots and the tail buffer repeat with this period in steps: a graph of a
+    // multiple of it continues the stream exactly on every launch
+    const long long ring_period = h->fbs / h->B;
+    const long long period = ring_period / gcd_ll(ring_period, 2) * 2;
+    if (nsteps <= 0 || nsteps % period != 0)
+        return h->fail(MSOSM_ERR_ARG, "nsteps must be a positive multiple of " + std::to_string(period) +
+                                          " (the ring's period in steps)");
+    msosm_graph_s *g = new (std::nothrow) msosm_graph_s();
+    if (!g)
+        return MSOSM_ERR_NOMEM;
+    g->h = h;
+    g->nsteps = nsteps;
+    cudaError_t e;
+    if (h->fold && (e = dalloc(&g->d_phase, 1)) != cudaSuccess)
+    {
+        delete g;
+        return h->cuda_fail(e, "cudaMalloc(graph phase)");
+    }
+    cudaStream_t cs = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)
+    {
+        delete g;
+        return h->cuda_fail(e, "cudaStreamCreate(capture)");
+    }
+    // host-side state the captured calls advance; restored afterwards (capture runs nothing)
+    const long long step0 = h->step;
+    const int tail0 = h->tail_cur;
+    const double t0 = h->fold ? h->fold->t_start : 0.0;
+    h->graph_phase = g->d_phase;
+    cudaGraph_t graph = nullptr;
+    int rc = MSOSM_OK;
+    const size_t step_bytes = (size_t)h->B * h->M * in_elem_bytes(h->in_format);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess)
+        rc = h->cuda_fail(e, "cudaStreamBeginCapture");
+    for (int s = 0; rc == MSOSM_OK && s < nsteps; s++)
+        rc = process_one(h, (const char *)in + (size_t)s * step_bytes, true, cs);
+    if (e == cudaSuccess)
+    {
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (rc == MSOSM_OK && e2 != cudaSuccess)
+            rc = h->cuda_fail(e2, "cudaStreamEndCapture");
+    }
+    if (rc == MSOSM_OK && (e = cudaGraphInstantiate(&g->exec, graph, 0)) != cudaSuccess)
+        rc = h->cuda_fail(e, "cudaGraphInstantiate");
+    if (graph)
+        cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    h->graph_phase = nullptr;
+    h->step = step0;
+    h->tail_cur = tail0;
+    if (h->fold)
+        h->fold->t_start = t0;
+    if (rc != MSOSM_OK)
+    {
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_graph_launch(msosm_graph_t *g, void *stream)
+{
+    if (!g || !g->h)
+        return MSOSM_ERR_ARG;
+    msosm_t *h = g->h;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e;
+    if (h->fold)
+    {
+        // the phase of this launch's first sample, as msosm_process would pass it
+        const msosm::FoldArgs fa = h->fold->args();
+        if ((e = msosm::launch_phase_set(g->d_phase, fa.phase0, st)) != cudaSuccess)
+            return h->cuda_fail(e, "fold phase set");
+    }
+    if ((e = cudaGraphLaunch(g->exec, st)) != cudaSuccess)
+        return h->cuda_fail(e, "cudaGraphLaunch");
+    h->step += g->nsteps;
+    h->tail_cur ^= (g->nsteps & 1);
+    if (h->fold)
+        h->fold->t_start += (double)g->nsteps * (double)((size_t)h->B * h->M) * h->fold->dt;
+    return MSOSM_OK;
+}
+
+extern "C" int msosm_graph_destroy(msosm_graph_t *g)
+{
+    if (!g)
+        return MSOSM_ERR_ARG;
+    delete g;
+    return MSOSM_OK;
 }
 
 extern "C" int msosm_process(msosm_t *h, const void *in, void *stream)

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(FOLD_THREADS)
                 p = x.x * x.x + x.y * x.y;
                 nz = p != 0.0f;
             }
-            bin = phase_bin(f.phase0 + (uint64_t)i * f.dphase, f.K);
+            bin = phase_bin(fold_phase0(f) + (uint64_t)i * f.dphase, f.K);
         }
         if constexpr (SMEM_BINS)
             fold_accumulate(s_sum, s_cnt, bin, p, nz);
@@ -149,6 +149,23 @@ cudaError_t launch_fold_finalize(const double *sum, const unsigned long long *cn
     if (n == 0)
         return cudaSuccess;
     fold_finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(sum, cnt, folded, n);
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void phase_set_kernel(unsigned long long *p, unsigned long long v) { *p = v; }
+__global__ void phase_advance_kernel(unsigned long long *p, unsigned long long inc) { *p += inc; }
+} // namespace
+
+cudaError_t launch_phase_set(uint64_t *phase, uint64_t value, cudaStream_t st)
+{
+    phase_set_kernel<<<1, 1, 0, st>>>(reinterpret_cast<unsigned long long *>(phase), value);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase_advance(uint64_t *phase, uint64_t inc, cudaStream_t st)
+{
+    phase_advance_kernel<<<1, 1, 0, st>>>(reinterpret_cast<unsigned long long *>(phase), inc);
     return cudaGetLastError();
 }
 

@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(TileCfg<N>::THREADS, TileCfg<N>::MIN_BLOCKS)
                          out_u16 ? out_u16 + row : nullptr,
                          s_sum,
                          s_cnt,
-                         fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * fold.dphase,
+                         fold_phase0(fold) + (uint64_t)((uint64_t)b * (uint64_t)M) * fold.dphase,
                          fold.dphase,
                          fold.K,
                          r0,

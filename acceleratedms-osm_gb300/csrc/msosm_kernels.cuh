@@ -44,16 +44,31 @@ struct FoldArgs
     uint64_t phase0;     // phase of sample 0 of this call, Q0.64 turns
     uint64_t dphase;     // phase advance per sample, Q0.64 turns
     unsigned K;          // bins per series
+    // set in captured graphs: phase0 is read from here at run time (the graph's calls
+    // advance it), since a replay cannot take a new phase0 from the host
+    const uint64_t *phase_dev = nullptr;
 };
 
-// Forward: B overlapping windows of the [tail | new input] stream -> spectra ring slots.
-// Pass 1 (decode + column transforms -> T), pass 2 (row transforms -> ring slot rbi+b).
+#ifdef __CUDACC__
+__device__ __forceinline__ uint64_t fold_phase0(const FoldArgs &f)
+{
+    return f.phase_dev ? __ldcg(reinterpret_cast<const unsigned long long *>(f.phase_dev)) : f.phase0;
+}
+#endif
+
+// Device-resident fold phase of captured graphs: set it (stream-ordered, no host buffer)
+// or advance it by one call's samples.
+cudaError_t launch_phase_set(uint64_t *phase, uint64_t value, cudaStream_t st);
+cudaError_t launch_phase_advance(uint64_t *phase, uint64_t inc, cudaStream_t st);
+
 // Which step of the last failed launch helper on this thread went wrong (the shared-
 // memory attribute or the launch itself, with the launch geometry); empty if none.
 const char *launch_failure_detail();
 void set_launch_failure_detail(const char *kernel, const char *step, unsigned gx, unsigned gy, unsigned block,
                                size_t smem);
 
+// Forward: B overlapping windows of the [tail | new input] stream -> spectra ring slots.
+// Pass 1 (decode + column transforms -> T), pass 2 (row transforms -> ring slot rbi+b).
 cudaError_t launch_forward_p1(const Geom &g, const Twiddles &tw, int in_format, const void *in, const float2 *tail,
                               float2 *tail_next, float2 *T, int B, cudaStream_t st);
 cudaError_t launch_forward_p2(const Geom &g, const Twiddles &tw, const float2 *T, float2 *ring, int rbi, int B,

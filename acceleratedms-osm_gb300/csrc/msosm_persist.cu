@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             if constexpr (FOLD)
             {
                 fold_tile<C2::COLS, N1 / 2>(s_p, s_bins,
-                                            a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
+                                            fold_phase0(a.fold) + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
                                             a.fold.dphase, a.fold.K, r0, N2);
                 // s_p and the bins are next touched after the next ticket barrier
             }
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
             {
                 __syncthreads();
                 fold_tile<TC_COLS, N1 / 2>(s_p, s_bins,
-                                          a.fold.phase0 + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
+                                          fold_phase0(a.fold) + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
                                           a.fold.dphase, a.fold.K, r0, N2);
             }
         }

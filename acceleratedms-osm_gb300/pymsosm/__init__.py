@@ -132,6 +132,9 @@ def _declare(L):
     L.msosm_plan_response.argtypes = [F, F, F, I, P]
     L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
     L.msosm_set_response.argtypes = [P, I, P]
+    L.msosm_graph_create.argtypes = [P, P, I, C.POINTER(P)]
+    L.msosm_graph_launch.argtypes = [P, P]
+    L.msosm_graph_destroy.argtypes = [P]
     L.msosm_writer_copy_output.argtypes = [P, P, P]
     ULL = C.c_ulonglong
     L.msosm_sim_create.argtypes = [F, F, F, F, C.POINTER(P)]
@@ -291,6 +294,13 @@ class MsosmGpuBatch:
         self._check(lib().msosm_set_precision(self._h, int(precision)))
         return self
 
+    def capture(self, data, nsteps: int) -> "StepGraph":
+        """A CUDA graph of the next `nsteps` steps reading device buffer `data`
+        (msosm_graph_create); launch() replays them as the following steps."""
+        g = P()
+        self._check(lib().msosm_graph_create(self._h, _ptr(data), int(nsteps), C.byref(g)))
+        return StepGraph(self, g, data)
+
     def launch_info(self) -> dict:
         """Geometry of the last persistent inverse-transform launch."""
         v = [C.c_int() for _ in range(4)]
@@ -368,6 +378,21 @@ class OsmGpuBatch(MsosmGpuBatch):
 
     def __init__(self, bw: float, dm: float, f0: float):
         super().__init__(bw, None, f0, _osm_dm=dm)
+
+
+class StepGraph:
+    """Captured steps of a processor (msosm_graph_*); keeps the processor and the input alive."""
+
+    def __init__(self, proc: MsosmGpuBatch, g, data):
+        self.proc, self._g, self._data = proc, g, data
+
+    def launch(self, stream=None):
+        self.proc._check(lib().msosm_graph_launch(self._g, _stream(stream)))
+
+    def __del__(self):
+        if getattr(self, "_g", None) and _lib is not None:
+            _lib.msosm_graph_destroy(self._g)
+            self._g = None
 
 
 SIM_TEST_PULSE, SIM_GAUSSIAN, SIM_IMPULSES = 0, 1, 2

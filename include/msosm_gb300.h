@@ -135,6 +135,23 @@ int msosm_process(msosm_t *h, const void *in, void *stream);
 /* `nsteps` consecutive steps from one contiguous input of nsteps*B*M samples. */
 int msosm_process_many(msosm_t *h, const void *in, int nsteps, void *stream);
 
+/* ---- CUDA-graph capture ---------------------------------------------------------
+ * No counterpart in the reference.  msosm_graph_create captures `nsteps` consecutive
+ * steps of the handle reading `in` (device memory, nsteps*B*M samples at a fixed
+ * address) into a CUDA graph: per step the forward passes, the one persistent inverse
+ * launch and, with a fold attached, a device-side advance of the fold's phase.
+ * msosm_graph_launch replays it on `stream` as the next nsteps steps (the caller
+ * refills `in` between launches): the ring slots and the tail buffer repeat, so nsteps
+ * must be a multiple of lcm(ring_blocks / B, 2), and the fold's time origin is set on
+ * the device at each launch, so folding continues as with msosm_process.  Needs
+ * fftpoint >= 65536, no writer and no kernel timing; the handle must not be
+ * destroyed before its graphs.  Capture runs nothing and leaves the handle's state
+ * as it was. */
+typedef struct msosm_graph_s msosm_graph_t;
+int msosm_graph_create(msosm_t *h, const void *in, int nsteps, msosm_graph_t **out);
+int msosm_graph_launch(msosm_graph_t *g, void *stream);
+int msosm_graph_destroy(msosm_graph_t *g);
+
 /* Copy the last step's [D][B][M] output (format = the init'ed out_mode's series,
  * complex64 if both) to `out` (host or device).  Replaces
  * MSOSM_GPU_BATCH::get_output(uint16_pair*) (msosm_gpu_batch.h:21, .cpp:238-245). */
