@@ -547,6 +547,23 @@ def run_engine(args, w, rank, world, local):
         "kernel_share": {k: v["ms"] / max(sum(p["ms"] for p in prof.values()), 1e-9) for k, v in prof.items()},
     }
 
+    # ---- the same steps replayed from a captured CUDA graph (msosm_graph_*) --
+    # (needs the ring's period in steps to divide the calls of a step: 2 here)
+    graph = proc.capture(dinp, calls)
+    graph.launch(stream)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        graph.launch(stream)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    g_ms = reduce_max(g0.elapsed_time(g1), world)
+    graph_line = {"value": total_units / (g_ms * 1e-3), "unit": UNIT, "ms_per_step": g_ms / args.steps,
+                  "calls_per_graph": calls,
+                  "note": "each step's forward passes and persistent inverse launches replayed from one graph"}
+    del graph
+
     # ---- end-to-end through the C ABI from pinned host memory -------------
     folded_host = np.zeros((len(dms), w["nbins"]), np.float32)
     proc.filter_blocks(host, calls, stream)  # one untimed e2e warm-up step
@@ -593,6 +610,7 @@ def run_engine(args, w, rank, world, local):
                    "l2": "inputs larger than L2 (512 MB baseband, 1 GB responses, 128 MB spectra ring)",
                    "parallelism": f"dm-shard x{world}"},
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "check": check,
+        "graph": graph_line,
     }
     if world == 1 and not args.no_cufft_baseline:
         line["reference_gpu_design"] = cufft_design_rate(proc, dms, dinp, w, calls, args.steps, stream,
