@@ -706,6 +706,17 @@ extern "C" int msosm_get_precision(const msosm_t *h)
     return h ? h->precision : -1;
 }
 
+extern "C" int msosm_reset_l2_persisting(void)
+{
+    const cudaError_t e = cudaCtxResetPersistingL2Cache();
+    if (e != cudaSuccess)
+    {
+        (void)cudaGetLastError();
+        return MSOSM_ERR_CUDA;
+    }
+    return MSOSM_OK;
+}
+
 extern "C" int msosm_get_launch_info(const msosm_t *h, int *grid, int *occupancy, int *lag, int *slots)
 {
     if (!h)

@@ -132,6 +132,7 @@ def _declare(L):
     L.msosm_plan_response.argtypes = [F, F, F, I, P]
     L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
     L.msosm_set_response.argtypes = [P, I, P]
+    L.msosm_reset_l2_persisting.argtypes = []
     L.msosm_graph_create.argtypes = [P, P, I, C.POINTER(P)]
     L.msosm_graph_launch.argtypes = [P, P]
     L.msosm_graph_destroy.argtypes = [P]
@@ -438,6 +439,12 @@ class Simulator:
         if getattr(self, "_h", None) and _lib is not None:
             _lib.msosm_sim_destroy(self._h)
             self._h = None
+
+
+def reset_l2_persisting() -> None:
+    """Return L2 lines marked persisting by the persistent transform to normal."""
+    if lib().msosm_reset_l2_persisting() != OK:
+        raise MsosmError("msosm_reset_l2_persisting")
 
 
 def awgn(n: int, mean: float = 0.0, stddev: float = 1.0, seed: int = 1, first: int = 0, out=None, stream=None):

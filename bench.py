@@ -617,6 +617,8 @@ def run_engine(args, w, rank, world, local):
         "graph": graph_line,
     }
     if world == 1 and not args.no_cufft_baseline:
+        torch.cuda.synchronize()
+        eng.reset_l2_persisting()  # the engine's persisting slot lines must not crowd the baseline's L2
         line["reference_gpu_design"] = cufft_design_rate(proc, dms, dinp, w, calls, args.steps, stream,
                                                          folded_host)
     if world == 1 and not args.no_cpu_baseline:

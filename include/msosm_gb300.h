@@ -107,6 +107,11 @@ int msosm_get_precision(const msosm_t *h);
  * slots; zeros before the first such launch.  No counterpart in the reference. */
 int msosm_get_launch_info(const msosm_t *h, int *grid, int *occupancy, int *lag, int *slots);
 
+/* Return the L2 lines that persistent launches marked persisting (their access-policy
+ * window over the intermediate slots) to normal, e.g. before timing other GPU work in
+ * the same process.  No counterpart in the reference. */
+int msosm_reset_l2_persisting(void);
+
 /* Planning results: M, M_min, F = 2M, batch, DM count, processor-wide delaycount
  * and the number of spectra kept in the ring (fft_block_size).  Any pointer may
  * be NULL.  Replaces the public members M, M_min, numDMs, delaycount of
