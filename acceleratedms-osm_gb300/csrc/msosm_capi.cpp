@@ -267,6 +267,7 @@ struct msosm_s
     unsigned *d_absmax = nullptr;
     float hmax = 1.0f;
     uint64_t *graph_phase = nullptr; // while capturing a graph: the fold's device-resident phase
+    int ctas_per_sm = 0;              // launch shape of the persistent transform (0 = as many as fit)
     float *pair_out = nullptr;      // first polarisation of a 2-pol fused fold: |a|^2 goes here
     const float *pair_in = nullptr; // second polarisation: folds sqrt(pair_in + |b|^2)
     Profiler prof;
@@ -708,12 +709,16 @@ extern "C" int msosm_get_precision(const msosm_t *h)
 
 extern "C" int msosm_reset_l2_persisting(void)
 {
-    const cudaError_t e = cudaCtxResetPersistingL2Cache();
-    if (e != cudaSuccess)
-    {
-        (void)cudaGetLastError();
-        return MSOSM_ERR_CUDA;
-    }
+    return msosm::persist_l2_reset() == cudaSuccess ? MSOSM_OK : MSOSM_ERR_CUDA;
+}
+
+extern "C" int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm)
+{
+    if (!h)
+        return MSOSM_ERR_ARG;
+    if (ctas_per_sm < 0 || ctas_per_sm > 4)
+        return h->fail(MSOSM_ERR_ARG, "ctas_per_sm must be 0 (as many as fit) .. 4");
+    h->ctas_per_sm = ctas_per_sm;
     return MSOSM_OK;
 }
 
@@ -909,6 +914,7 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         pa.p2_done = h->d_sync + 1 + kMaxSlots;
         pa.err = h->d_err;
         pa.timeout_ns = kWaitTimeoutNs;
+        pa.max_ctas_per_sm = h->ctas_per_sm;
         msosm::TcArgs tc{static_cast<const uint4 *>(h->d_tc_op), h->d_absmax, h->hmax};
         const bool use_tc = h->precision != msosm::PREC_FP32;
         msosm::PersistPlan plan;
@@ -1331,6 +1337,104 @@ extern "C" int msosm_autotune(float bw, float f0, const float *dms, int num_dms,
     if (best_rate)
         *best_rate = best_r;
     return MSOSM_OK;
+}
+
+extern "C" int msosm_autotune_shape(float bw, float f0, const float *dms, int num_dms, int in_format,
+                                    int min_fftpoint, int max_fftpoint, const int *batches, int num_batches,
+                                    int steps, int *best_fftpoint, int *best_batch, int *best_ctas_per_sm,
+                                    double *best_rate)
+{
+    if (!dms || num_dms <= 0 || !batches || num_batches <= 0 || steps <= 0 || !best_fftpoint || !best_batch ||
+        !best_ctas_per_sm || in_elem_bytes(in_format) == 0)
+        return MSOSM_ERR_ARG;
+    std::vector<float> sub;
+    const int nsub = std::min(num_dms, 16);
+    for (int i = 0; i < nsub; i++)
+        sub.push_back(dms[(long long)i * (num_dms - 1) / std::max(1, nsub - 1)]);
+    sub.back() = dms[num_dms - 1];
+    std::sort(sub.begin(), sub.end());
+    int mmin = 0;
+    for (float d : sub)
+        mmin = std::max(mmin, msosm::plan_min_order(msosm::plan_nd(bw, d, f0)));
+    const long long lo = std::max<long long>(std::max(min_fftpoint, 1 << kMinLog2F), 2ll * mmin);
+    const long long hi = std::min<long long>(max_fftpoint, 1ll << kMaxLog2F);
+    double best_r = 0.0;
+    *best_fftpoint = *best_batch = *best_ctas_per_sm = 0;
+    for (long long F = 1; F <= hi; F <<= 1)
+    {
+        if (F < lo)
+            continue;
+        for (int bi = 0; bi < num_batches; bi++)
+        {
+            const int batch = batches[bi];
+            if (batch <= 0)
+                continue;
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            const int dc = msosm::plan_delaycount(msosm::plan_nd(bw, sub.back(), f0), (int)(F / 2));
+            const double need = (double)F * 8 * (dc + 2 * batch + 64) + (double)sub.size() * F * 10 +
+                                (double)batch * F / 2 * in_elem_bytes(in_format) * 2;
+            if (need > 0.8 * (double)free_b)
+                continue;
+            // launch shapes: as many CTAs per SM as fit, then one (persistent sizes only)
+            for (int ctas : {0, 1})
+            {
+                if (ctas == 1 && F < (1 << 16))
+                    continue;
+                msosm_t *h = nullptr;
+                if (msosm_create(bw, f0, sub.data(), (int)sub.size(), &h) != MSOSM_OK)
+                    continue;
+                int rc = msosm_init(h, (int)F, batch, in_format, MSOSM_OUT_NONE);
+                if (rc == MSOSM_OK)
+                    rc = msosm_set_launch_shape(h, ctas);
+                msosm_fold_t *f = nullptr;
+                if (rc == MSOSM_OK)
+                    rc = msosm_fold_create(1.0f, bw, (unsigned long)batch * (F / 2), 64, (int)sub.size(), &f);
+                if (rc == MSOSM_OK)
+                    rc = msosm_attach_fold(h, f);
+                void *in = nullptr;
+                const size_t in_bytes = (size_t)batch * (F / 2) * in_elem_bytes(in_format);
+                cudaEvent_t e0 = nullptr, e1 = nullptr;
+                if (rc == MSOSM_OK && cudaMalloc(&in, in_bytes) == cudaSuccess &&
+                    cudaMemset(in, 0, in_bytes) == cudaSuccess && cudaEventCreate(&e0) == cudaSuccess &&
+                    cudaEventCreate(&e1) == cudaSuccess)
+                {
+                    rc = msosm_process(h, in, nullptr); // warm-up
+                    cudaEventRecord(e0, nullptr);
+                    for (int s = 0; rc == MSOSM_OK && s < steps; s++)
+                        rc = msosm_process(h, in, nullptr);
+                    cudaEventRecord(e1, nullptr);
+                    if (rc == MSOSM_OK)
+                        rc = msosm_sync(h, nullptr);
+                    float ms = 0.f;
+                    if (rc == MSOSM_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0.f)
+                    {
+                        const double rate = (double)steps * batch * (F / 2) * sub.size() / (ms * 1e-3);
+                        if (rate > best_r)
+                        {
+                            best_r = rate;
+                            *best_fftpoint = (int)F;
+                            *best_batch = batch;
+                            *best_ctas_per_sm = ctas;
+                        }
+                    }
+                }
+                cudaGetLastError();
+                if (e0)
+                    cudaEventDestroy(e0);
+                if (e1)
+                    cudaEventDestroy(e1);
+                if (in)
+                    cudaFree(in);
+                msosm_destroy(h);
+                if (f)
+                    msosm_fold_destroy(f);
+            }
+        }
+    }
+    if (best_rate)
+        *best_rate = best_r;
+    return *best_fftpoint ? MSOSM_OK : MSOSM_ERR_UNSUPPORTED;
 }
 
 // ---- DM derivative ------------------------------------------------------------------

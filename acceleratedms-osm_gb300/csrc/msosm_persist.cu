@@ -845,25 +845,22 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
         umma::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
-// Raise (never lower) this device's persisting-L2 set-aside to `bytes`, capped at the
-// device maximum, once per size.  A failure only costs the hint.
+// This device's persisting-L2 set-aside for the slot ring of the launch at hand: set
+// to `bytes` (capped at the device maximum) whenever a launch needs another size, so a
+// large ring (e.g. a simulator's filter) does not keep L2 set aside for later work.  A
+// failure only costs the hint.
+size_t g_l2_set[kMaxDevices] = {};
+
 void ensure_l2_persisting(size_t bytes)
 {
-    static size_t done[kMaxDevices] = {};
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices || done[dev] >= bytes)
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices || g_l2_set[dev] == bytes)
         return;
     int maxp = 0;
-    size_t cur = 0;
-    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
-        cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) == cudaSuccess)
-    {
-        const size_t want = std::min((size_t)maxp, bytes);
-        if (want > cur)
-            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);
-    }
+    if (cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess)
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min((size_t)maxp, bytes));
     cudaGetLastError();
-    done[dev] = bytes;
+    g_l2_set[dev] = bytes;
 }
 
 // Launch (or, with `plan`, only size) a persistent transform kernel `k` taking
@@ -896,6 +893,8 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
     // for room for carveout_blocks CTAs is launched with that many per SM (the
     // ticket order is deadlock-free whatever the residency)
     per_sm = std::min(std::max(per_sm, carveout_blocks), max_per_sm);
+    if (a.max_ctas_per_sm > 0)
+        per_sm = std::min(per_sm, a.max_ctas_per_sm);
     if (per_sm < 1)
         return cudaErrorInvalidConfiguration;
     const int grid = per_sm * sms;
@@ -1106,6 +1105,23 @@ cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned lon
 }
 
 bool persist_supported(int L) { return L >= 16 && L <= 24; }
+
+cudaError_t persist_l2_reset()
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = cudaCtxResetPersistingL2Cache()) != cudaSuccess ||
+        (e = cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0)) != cudaSuccess)
+    {
+        (void)cudaGetLastError();
+        return e;
+    }
+    if (dev >= 0 && dev < kMaxDevices)
+        g_l2_set[dev] = 0;
+    return cudaSuccess;
+}
 
 cudaError_t persist_plan(int L, const PersistArgs &a, int sms, PersistPlan *plan)
 {

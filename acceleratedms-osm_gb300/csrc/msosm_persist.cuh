@@ -25,6 +25,7 @@ struct PersistArgs
     unsigned *p2_done; // [S], zeroed before the launch
     int *err;          // sticky error flag (1 = a wait timed out)
     unsigned long long timeout_ns;
+    int max_ctas_per_sm; // host side: cap on resident CTAs per SM of the launch (0 = as many as fit)
 };
 
 // Split-precision transform (tensor cores): precisions and extra arguments.
@@ -49,6 +50,9 @@ struct PersistPlan
 };
 
 bool persist_supported(int L);
+// Return persisting L2 lines to normal and the persisting set-aside to zero (the next
+// persistent launch sets it again for its slot ring).
+cudaError_t persist_l2_reset();
 // The persistent kernel's bounded wait, run alone (see msosm_selftest_wait).
 cudaError_t persist_selftest_wait(unsigned preset, unsigned target, unsigned long long timeout_ns, int *timed_out,
                                   unsigned long long *elapsed_ns);

@@ -132,6 +132,7 @@ def _declare(L):
     L.msosm_plan_response.argtypes = [F, F, F, I, P]
     L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
     L.msosm_set_response.argtypes = [P, I, P]
+    L.msosm_set_launch_shape.argtypes = [P, I]
     L.msosm_reset_l2_persisting.argtypes = []
     L.msosm_graph_create.argtypes = [P, P, I, C.POINTER(P)]
     L.msosm_graph_launch.argtypes = [P, P]
@@ -301,6 +302,11 @@ class MsosmGpuBatch:
         g = P()
         self._check(lib().msosm_graph_create(self._h, _ptr(data), int(nsteps), C.byref(g)))
         return StepGraph(self, g, data)
+
+    def set_launch_shape(self, ctas_per_sm: int) -> "MsosmGpuBatch":
+        """At most ctas_per_sm resident CTAs per SM for the persistent transform (0 = all that fit)."""
+        self._check(lib().msosm_set_launch_shape(self._h, int(ctas_per_sm)))
+        return self
 
     def launch_info(self) -> dict:
         """Geometry of the last persistent inverse-transform launch."""
@@ -622,6 +628,23 @@ def autotune(bw, f0, dms, batch, in_format=IN_C64, min_fftpoint=1 << 16, max_fft
         table[key] = {"fftpoint": best.value, "rate": rate.value}
         p.write_text(json.dumps(table, indent=1))
     return best.value, rate.value
+
+
+def autotune_shape(bw, f0, dms, batches=(2, 4, 8, 16, 32), in_format=IN_C64, min_fftpoint=1 << 16,
+                   max_fftpoint=1 << 20, steps=3) -> dict:
+    """Fastest (fftpoint, batch, CTAs per SM) for this DM list on this GPU
+    (msosm_autotune_shape)."""
+    d = np.ascontiguousarray(np.sort(np.atleast_1d(np.asarray(dms, np.float32))))
+    bs = np.ascontiguousarray(np.asarray(batches, np.int32))
+    out = [C.c_int() for _ in range(3)]
+    rate = C.c_double()
+    L = lib()
+    L.msosm_autotune_shape.argtypes = [F, F, P, I, I, I, I, P, I, I, PI, PI, PI, C.POINTER(C.c_double)]
+    rc = L.msosm_autotune_shape(bw, f0, d.ctypes.data, len(d), in_format, min_fftpoint, max_fftpoint, bs.ctypes.data,
+                                len(bs), steps, *[C.byref(v) for v in out], C.byref(rate))
+    if rc != OK:
+        raise MsosmError(f"autotune_shape: {L.msosm_status_string(rc).decode()}")
+    return {"fftpoint": out[0].value, "batch": out[1].value, "ctas_per_sm": out[2].value, "rate": rate.value}
 
 
 def selftest_wait(preset: int, target: int, timeout_ns: int) -> tuple[bool, int]:

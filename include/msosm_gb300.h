@@ -108,8 +108,11 @@ int msosm_get_precision(const msosm_t *h);
 int msosm_get_launch_info(const msosm_t *h, int *grid, int *occupancy, int *lag, int *slots);
 
 /* Return the L2 lines that persistent launches marked persisting (their access-policy
- * window over the intermediate slots) to normal, e.g. before timing other GPU work in
- * the same process.  No counterpart in the reference. */
+ * window over the intermediate slots) to normal and this context's persisting set-aside
+ * to zero, e.g. before timing other GPU work in the same process; the next persistent
+ * launch sets the set-aside again for its own slot ring (each launch sets it to the size
+ * its ring needs).  Context state only, gone with the process.  No counterpart in the
+ * reference. */
 int msosm_reset_l2_persisting(void);
 
 /* Planning results: M, M_min, F = 2M, batch, DM count, processor-wide delaycount
@@ -202,6 +205,18 @@ int msosm_profile_read(msosm_t *h, int kind, double *ms_total, long long *launch
  * fastest in samples x DM trials per second.  The caller caches the answer. */
 int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch, int in_format, int min_fftpoint,
                    int max_fftpoint, int steps, int *best_fftpoint, double *best_rate);
+
+/* Launch shape of the persistent inverse transform: at most ctas_per_sm resident CTAs per
+ * SM (0, the default, = as many as fit).  Fewer CTAs keep fewer intermediate slots in
+ * flight (less L2 pressure at large F).  No counterpart in the reference. */
+int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm);
+/* msosm_autotune over the FFT size, the windows per call (`batches`, num_batches
+ * candidates) and the launch shape (as many CTAs per SM as fit, or one), fold-only on
+ * at most 16 of the DMs; the fastest triple and its rate.  The radix plan and tile of
+ * each size are fixed (one measured plan per size). */
+int msosm_autotune_shape(float bw, float f0, const float *dms, int num_dms, int in_format, int min_fftpoint,
+                         int max_fftpoint, const int *batches, int num_batches, int steps, int *best_fftpoint,
+                         int *best_batch, int *best_ctas_per_sm, double *best_rate);
 
 /* Failure-detection self-test (no counterpart in the reference): runs the persistent
  * transform's bounded device-side wait alone, on a counter preset to `preset` that

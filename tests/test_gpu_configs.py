@@ -196,3 +196,18 @@ def test_two_pol_int8_full_size(eng, orc):
                 r[:, j * step:(j + 1) * step] = o.reshape(len(pick), -1)
         for k in range(len(pick)):
             assert rel_l2(got[p][k], r[k]) < 1e-4, (p, k, float(dms[pick[k]]))
+
+
+def test_autotune_shape_picks_a_valid_triple(eng):
+    bw, f0 = np.float32(128e6), np.float32(756e6)
+    rng = np.random.default_rng(4)
+    dms = np.sort(np.exp(rng.uniform(np.log(1.0), np.log(1000.0), 1024))).astype(np.float32)
+    best = eng.autotune_shape(bw, f0, dms, batches=(2, 8), in_format=eng.IN_I8, min_fftpoint=1 << 16,
+                              max_fftpoint=1 << 20, steps=2)
+    print("autotune_shape:", best)
+    assert best["fftpoint"] == 1 << 20  # the largest DM forces F = 2^20
+    assert best["batch"] in (2, 8) and best["ctas_per_sm"] in (0, 1) and best["rate"] > 0
+    m = eng.MsosmGpuBatch(bw, dms[:4], f0).initialize(1 << 20, 2, eng.IN_I8, eng.OUT_C64).set_launch_shape(1)
+    m.filter_block(np.zeros(2 * 2 * m.M, np.int8))
+    m.synchronize()
+    assert m.launch_info()["grid"] == 152 or m.launch_info()["grid"] <= 2 * 152
