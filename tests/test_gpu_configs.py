@@ -210,4 +210,5 @@ def test_autotune_shape_picks_a_valid_triple(eng):
     m = eng.MsosmGpuBatch(bw, dms[:4], f0).initialize(1 << 20, 2, eng.IN_I8, eng.OUT_C64).set_launch_shape(1)
     m.filter_block(np.zeros(2 * 2 * m.M, np.int8))
     m.synchronize()
-    assert m.launch_info()["grid"] == 152 or m.launch_info()["grid"] <= 2 * 152
+    torch = pytest.importorskip("torch")
+    assert m.launch_info()["grid"] == torch.cuda.get_device_properties(0).multi_processor_count
