@@ -268,6 +268,7 @@ struct msosm_s
     float hmax = 1.0f;
     uint64_t *graph_phase = nullptr; // while capturing a graph: the fold's device-resident phase
     int ctas_per_sm = 0;              // launch shape of the persistent transform (0 = as many as fit)
+    int dm_group = 1;                 // transform order: DM trials per window-major group
     float *pair_out = nullptr;      // first polarisation of a 2-pol fused fold: |a|^2 goes here
     const float *pair_in = nullptr; // second polarisation: folds sqrt(pair_in + |b|^2)
     Profiler prof;
@@ -712,13 +713,17 @@ extern "C" int msosm_reset_l2_persisting(void)
     return msosm::persist_l2_reset() == cudaSuccess ? MSOSM_OK : MSOSM_ERR_CUDA;
 }
 
-extern "C" int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm)
+extern "C" int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm, int dm_group)
 {
     if (!h)
         return MSOSM_ERR_ARG;
     if (ctas_per_sm < 0 || ctas_per_sm > 4)
         return h->fail(MSOSM_ERR_ARG, "ctas_per_sm must be 0 (as many as fit) .. 4");
+    if (dm_group < 0)
+        return h->fail(MSOSM_ERR_ARG, "dm_group must be >= 0");
     h->ctas_per_sm = ctas_per_sm;
+    if (dm_group > 0)
+        h->dm_group = dm_group;
     return MSOSM_OK;
 }
 
@@ -915,6 +920,8 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         pa.err = h->d_err;
         pa.timeout_ns = kWaitTimeoutNs;
         pa.max_ctas_per_sm = h->ctas_per_sm;
+        pa.D = h->D;
+        pa.dm_group = std::max(1, std::min(h->dm_group, h->D));
         msosm::TcArgs tc{static_cast<const uint4 *>(h->d_tc_op), h->d_absmax, h->hmax};
         const bool use_tc = h->precision != msosm::PREC_FP32;
         msosm::PersistPlan plan;
@@ -1386,7 +1393,7 @@ extern "C" int msosm_autotune_shape(float bw, float f0, const float *dms, int nu
                     continue;
                 int rc = msosm_init(h, (int)F, batch, in_format, MSOSM_OUT_NONE);
                 if (rc == MSOSM_OK)
-                    rc = msosm_set_launch_shape(h, ctas);
+                    rc = msosm_set_launch_shape(h, ctas, 0);
                 msosm_fold_t *f = nullptr;
                 if (rc == MSOSM_OK)
                     rc = msosm_fold_create(1.0f, bw, (unsigned long)batch * (F / 2), 64, (int)sub.size(), &f);

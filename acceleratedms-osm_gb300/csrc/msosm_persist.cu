@@ -326,6 +326,28 @@ __device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, i
     }
 }
 
+// Transform index gi -> (DM trial d, window b): DM trials in groups of G, window-major
+// inside a group (G = 1: DM-major), the last group holding the D mod G remaining trials.
+// Consecutive transforms then gather from nearly the same spectra-ring lines (neighbouring
+// trials' block delays differ by at most a step), which L2 serves to the whole group.
+__device__ __forceinline__ void transform_dm_window(unsigned gi, unsigned B, unsigned D, unsigned G, int &d, int &b)
+{
+    const unsigned full = D / G, per = G * B;
+    const unsigned grp = gi / per;
+    if (grp < full)
+    {
+        const unsigned r = gi - grp * per;
+        b = (int)(r / G);
+        d = (int)(grp * G + r % G);
+    }
+    else
+    {
+        const unsigned rem = D - full * G, r = gi - full * per;
+        b = (int)(r / rem);
+        d = (int)(full * G + r % rem);
+    }
+}
+
 // Thread 0 of a CTA: take the ticket it holds (fetching the next one, whose latency
 // overlaps the item), wait for the item's dependences, and return the verdict:
 // -1 stop (tickets exhausted; or, with stop_on_error, the launch failed), 0 skip
@@ -431,7 +453,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         const int slot = (int)((unsigned)f % (unsigned)a.S);
         float2 *Ts = a.T + (size_t)slot * F;
         const long long gi = a.g0 + f;
-        const int d = (int)((unsigned)gi / (unsigned)B), b = (int)((unsigned)gi % (unsigned)B);
+        int d, b;
+        transform_dm_window((unsigned)gi, (unsigned)B, (unsigned)a.D, (unsigned)a.dm_group, d, b);
         if (is_p1)
         {
             const int c0 = w * C1::COLS;
@@ -691,7 +714,8 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_tc_kernel(PersistArgs a, TcA
         const int slot = (int)((unsigned)f % (unsigned)a.S);
         float2 *Ts = a.T + (size_t)slot * F;
         const long long gi = a.g0 + f;
-        const int d = (int)((unsigned)gi / (unsigned)B), b = (int)((unsigned)gi % (unsigned)B);
+        int d, b;
+        transform_dm_window((unsigned)gi, (unsigned)B, (unsigned)a.D, (unsigned)a.dm_group, d, b);
         float2 x[2][16];
         if (is_p1)
         {
@@ -911,7 +935,9 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
         plan->occupancy = occupancy;
         return cudaSuccess;
     }
-    // the kernel indexes transforms and tickets in 32 bits
+    // the kernel indexes transforms and tickets in 32 bits; its (d, b) map covers D * B
+    if (a.dm_group < 1 || a.D < 1 || a.g0 + a.G > (long long)a.D * a.B)
+        return cudaErrorInvalidValue;
     if (a.S <= a.lag || a.g0 < 0 || a.G < 0 || a.g0 + a.G + a.lag >= (1ll << 31) ||
         (a.G + a.lag) * (long long)per_block >= (1ll << 32))
         return cudaErrorInvalidValue;

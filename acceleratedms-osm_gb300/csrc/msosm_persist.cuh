@@ -26,6 +26,9 @@ struct PersistArgs
     int *err;          // sticky error flag (1 = a wait timed out)
     unsigned long long timeout_ns;
     int max_ctas_per_sm; // host side: cap on resident CTAs per SM of the launch (0 = as many as fit)
+    // transform order: groups of dm_group DM trials, window-major inside a group, so that
+    // consecutive transforms read the same ring slots (D = number of DM trials)
+    int D, dm_group;
 };
 
 // Split-precision transform (tensor cores): precisions and extra arguments.

@@ -132,7 +132,7 @@ def _declare(L):
     L.msosm_plan_response.argtypes = [F, F, F, I, P]
     L.osm_plan.argtypes = [F, F, F, C.POINTER(UL), C.POINTER(UL)]
     L.msosm_set_response.argtypes = [P, I, P]
-    L.msosm_set_launch_shape.argtypes = [P, I]
+    L.msosm_set_launch_shape.argtypes = [P, I, I]
     L.msosm_reset_l2_persisting.argtypes = []
     L.msosm_graph_create.argtypes = [P, P, I, C.POINTER(P)]
     L.msosm_graph_launch.argtypes = [P, P]
@@ -303,9 +303,10 @@ class MsosmGpuBatch:
         self._check(lib().msosm_graph_create(self._h, _ptr(data), int(nsteps), C.byref(g)))
         return StepGraph(self, g, data)
 
-    def set_launch_shape(self, ctas_per_sm: int) -> "MsosmGpuBatch":
-        """At most ctas_per_sm resident CTAs per SM for the persistent transform (0 = all that fit)."""
-        self._check(lib().msosm_set_launch_shape(self._h, int(ctas_per_sm)))
+    def set_launch_shape(self, ctas_per_sm: int = 0, dm_group: int = 0) -> "MsosmGpuBatch":
+        """Persistent transform: at most ctas_per_sm resident CTAs per SM (0 = all that fit)
+        and DM trials in window-major groups of dm_group (0 = keep)."""
+        self._check(lib().msosm_set_launch_shape(self._h, int(ctas_per_sm), int(dm_group)))
         return self
 
     def launch_info(self) -> dict:

@@ -384,7 +384,7 @@ def run_two_pol(args, w, rank, world, local):
     hosts = [torch.from_numpy(int8_baseband(N, w["sigma"], 40 + 2 * rank + p)).pin_memory() for p in range(2)]
     devs = [h.to(dev) for h in hosts]
     procs = [eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_I8, eng.OUT_NONE)
-             .set_launch_shape(args.ctas_per_sm) for _ in range(2)]
+             .set_launch_shape(args.ctas_per_sm, args.dm_group) for _ in range(2)]
     step_n = procs[0].batch * procs[0].M
     calls = N // step_n
     fold = eng.FoldGpu(np.float32(w["period"]), bw, step_n, w["nbins"], len(dms))
@@ -491,7 +491,7 @@ def run_engine(args, w, rank, world, local):
     host = dinp.cpu().pin_memory()
 
     proc = eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_C64, eng.OUT_NONE)
-    proc.set_launch_shape(args.ctas_per_sm)
+    proc.set_launch_shape(args.ctas_per_sm, args.dm_group)
     proc.set_precision(PRECISIONS[args.precision])
     step_n = proc.batch * proc.M
     calls = N // step_n
@@ -717,6 +717,8 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="override the windows per call")
     ap.add_argument("--ctas-per-sm", type=int, default=0,
                     help="cap on resident CTAs per SM of the persistent transform (0 = as many as fit)")
+    ap.add_argument("--dm-group", type=int, default=0,
+                    help="DM trials per window-major group of the persistent transform's order (0 = default)")
     ap.add_argument("--precision", default="fp32", choices=sorted(PRECISIONS),
                     help="inverse-transform arithmetic: fp32 register DFTs, or tensor-core DFT stages on "
                          "split bf16/fp16 operands (bf16x3 / fp16x3)")

@@ -207,9 +207,12 @@ int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch,
                    int max_fftpoint, int steps, int *best_fftpoint, double *best_rate);
 
 /* Launch shape of the persistent inverse transform: at most ctas_per_sm resident CTAs per
- * SM (0, the default, = as many as fit).  Fewer CTAs keep fewer intermediate slots in
- * flight (less L2 pressure at large F).  No counterpart in the reference. */
-int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm);
+ * SM (0, the default, = as many as fit; fewer CTAs keep fewer intermediate slots in
+ * flight, less L2 pressure at large F), and the transform order: DM trials in groups of
+ * dm_group, window-major inside a group, so that consecutive transforms gather from
+ * nearly the same spectra-ring lines (0 keeps the current order; 1 = DM-major).  Outputs
+ * do not depend on either.  No counterpart in the reference. */
+int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm, int dm_group);
 /* msosm_autotune over the FFT size, the windows per call (`batches`, num_batches
  * candidates) and the launch shape (as many CTAs per SM as fit, or one), fold-only on
  * at most 16 of the DMs; the fastest triple and its rate.  The radix plan and tile of

@@ -352,3 +352,34 @@ def test_linearity_at_full_size(eng):
     expect = 2.0 * runs[0].astype(np.complex128) - 3.0 * runs[1].astype(np.complex128)
     for d in range(len(dms)):
         assert rel_l2(runs[2][d], expect[d]) < 1e-5
+
+
+@pytest.mark.parametrize("group", [4, 8, 13, 32])
+def test_transform_order_does_not_change_outputs(eng, group):
+    """msosm_set_launch_shape's DM grouping (window-major groups, the last one partial)
+    and one CTA per SM give the DM-major order's series bit for bit, and its folds to
+    the fused fold's float-sum order."""
+    bw, f0 = np.float32(64e6), np.float32(1368e6)
+    dms = np.linspace(20.0, 180.0, 13).astype(np.float32)
+    F, B, K = 1 << 18, 4, 128
+    procs, folds = [], []
+    for g, ctas in ((1, 0), (group, 0), (group, 1)):
+        m = eng.MsosmGpuBatch(bw, dms, f0).initialize(F, B, eng.IN_C64, eng.OUT_C64).set_launch_shape(ctas, g)
+        f = eng.FoldGpu(np.float32(0.0047), bw, B * m.M, K, len(dms))
+        m.attach_fold(f)
+        procs.append(m)
+        folds.append(f)
+    rng = np.random.default_rng(group)
+    outs = [np.zeros((len(dms), B, procs[0].M), np.complex64) for _ in procs]
+    for s in range(3):
+        x = (rng.standard_normal(B * procs[0].M) + 1j * rng.standard_normal(B * procs[0].M)).astype(np.complex64)
+        for m, o in zip(procs, outs):
+            m.filter_block(x)
+            m.get_output(o)
+            m.synchronize()
+        assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    ref = folds[0].read()
+    for f in folds[1:]:
+        _, sums, cnts = f.read()
+        assert np.array_equal(cnts, ref[2])
+        assert rel_l2(sums, ref[1]) < 1e-6
