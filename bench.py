@@ -358,6 +358,37 @@ def cufft_design_rate(proc, dms, dinp, w, calls, steps, stream):
             "timed": "before the engine's launches, with no L2 set aside for persisting lines", "_folded": folded}
 
 
+def reference_shaped_rate(eng, bw, f0, dms, w, dinp, calls, steps, stream):
+    """The engine used the way the reference's programs use their processor: the series of
+    every DM written (complex64, fold mode), then a separate fold pass over it (Fold_GPU's
+    calculate_intensity + fold_data_phase), instead of the fused fold-only transform.  Same
+    workload, device-resident input, CUDA events."""
+    import torch
+
+    p = eng.MsosmGpuBatch(bw, dms, f0).initialize(w["fftpoint"], w["batch"], eng.IN_C64, eng.OUT_C64)
+    n = p.batch * p.M
+    fold = eng.FoldGpu(np.float32(w["period"]), bw, n, w["nbins"], len(dms))
+
+    def step():
+        fold.reset(stream)
+        for c in range(calls):
+            p.filter_block(dinp[2 * c * n:2 * (c + 1) * n], stream)
+            fold.accumulate(p.get_output_pointer(), None, stream)
+
+    step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_ms = e0.elapsed_time(e1)
+    del p, fold
+    return {"value": calls * n * len(dms) * steps / (t_ms * 1e-3), "unit": UNIT, "ms_per_step": t_ms / steps,
+            "kind": "series of every DM to HBM (complex64), then the stand-alone fold over it"}
+
+
 def int8_baseband(n, sigma, seed):
     """n complex samples of int8 interleaved I/Q: N(0, sigma^2) rounded, clipped to +-127."""
     rng = np.random.default_rng(seed)
@@ -624,6 +655,8 @@ def run_engine(args, w, rank, world, local):
         "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "check": check,
         "graph": graph_line,
     }
+    if world == 1 and not args.no_cufft_baseline:
+        line["reference_shaped_form"] = reference_shaped_rate(eng, bw, f0, dms, w, dinp, calls, args.steps, stream)
     if base is not None:
         if "_folded" in base:
             f = base.pop("_folded")
