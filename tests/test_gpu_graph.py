@@ -51,3 +51,24 @@ def test_graph_replays_equal_process_calls(eng, precision):
     assert np.abs(ca.astype(np.int64) - cg.astype(np.int64)).sum() <= 2 * len(dms)
     assert rel_l2(sg, sa) < 1e-6
     assert a.steps == g.steps == launches * nsteps
+
+
+def test_graph_capture_refuses_what_it_cannot_replay(eng):
+    torch = pytest.importorskip("torch")
+    bw, f0 = np.float32(64e6), np.float32(1368e6)
+    m = eng.MsosmGpuBatch(bw, [100.0, 120.0], f0).initialize(1 << 18, 4, eng.IN_C64, eng.OUT_C64)
+    rp = m.ring_blocks // 4
+    period = rp * 2 // np.gcd(rp, 2)
+    buf = torch.zeros(period * 4 * m.M, dtype=torch.complex64, device="cuda")
+    with pytest.raises(eng.MsosmError):
+        m.capture(buf, period + 1)  # not a multiple of the ring's period
+    with pytest.raises(eng.MsosmError):
+        m.capture(np.zeros(period * 4 * m.M, np.complex64), period)  # host input
+    small = eng.MsosmGpuBatch(bw, [1.0], f0).initialize(1 << 12, 4, eng.IN_C64, eng.OUT_C64)
+    with pytest.raises(eng.MsosmError):
+        small.capture(buf, 2)  # below the persistent transform's sizes
+    g = m.capture(buf, period)  # and the handle still processes normally afterwards
+    m.filter_block(buf[:4 * m.M])
+    m.synchronize()
+    assert m.steps == 1
+    del g

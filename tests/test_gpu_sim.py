@@ -108,3 +108,25 @@ def test_dedispersion_recovers_the_simulated_pulse(eng):
     assert snr[best] > 30
     # the smear at DM 50 is 7 % of the period: trials far from it lose much of the S/N
     assert snr[0] < 0.7 * snr[best] and snr[-1] < 0.7 * snr[best]
+
+
+def test_simulator_refuses_bad_requests(eng):
+    with pytest.raises(eng.MsosmError):
+        eng.Simulator(np.float32(16e6), np.float32(1392e6), np.float32(-1.0), np.float32(0.033))
+    with pytest.raises(eng.MsosmError):
+        eng.Simulator(np.float32(16e6), np.float32(1392e6), np.float32(5.0), np.float32(0.001), kind=7)
+    with pytest.raises(eng.MsosmError):
+        eng.Simulator(np.float32(16e6), np.float32(1392e6), np.float32(5.0), np.float32(0.001),
+                      kind=eng.SIM_GAUSSIAN, duty=1.5)
+    s = eng.Simulator(np.float32(16e6), np.float32(1392e6), np.float32(5.0), np.float32(0.001))
+    s.generate(1000)
+    L = eng.lib()
+    for call in (lambda: L.msosm_sim_set_seed(s._h, 3), lambda: L.msosm_sim_set_noise(s._h, 1, 0.0),
+                 lambda: L.msosm_sim_set_pulse(s._h, eng.SIM_IMPULSES, 0.05)):
+        with pytest.raises(eng.MsosmError, match="after the first generate"):
+            s._check(call())  # the signal model is fixed once generation started
+    assert s.position == 1000
+    # a smear of 2^23 samples or more would need a transform above 2^24 points
+    big = eng.Simulator(np.float32(128e6), np.float32(756e6), np.float32(1000.0), np.float32(0.01))
+    with pytest.raises(eng.MsosmError):
+        big.generate(10)
