@@ -100,12 +100,14 @@ __device__ __forceinline__ int ld_na(const uint16_t *p)
     return (int)v;
 }
 
+template <class HOOK>
 struct PInvLoader
 {
     const float2 *ring;
     const float2 *Hd;
     const uint16_t *dl;
     int c0, N1, F, fbs, rb;
+    HOOK hook; // run once all of this thread's loads are issued
     // The first stage's inputs in two waves: every delay, then every spectrum and
     // response value, so the delay -> spectrum dependences overlap across elements.
     template <int BPT, int R, int STRIDE, int COLS, int THREADS>
@@ -136,6 +138,7 @@ struct PInvLoader
                 v[i][r] = cmul(ld_na(ring + (size_t)s * F + n), ld_na(Hd + n));
             }
         }
+        hook();
     }
 };
 
@@ -170,10 +173,12 @@ struct PStoreT
 
 // Pass-2 inputs of row tile r0 .. r0+COLS-1 from the column-major slot: element
 // (row r0 + col, n1) at n1*N2 + r0 + col.  L2-resident, so loaded with .cg.
+template <class HOOK>
 struct PTLoader
 {
     const float2 *Ts;
     int r0, N2;
+    HOOK hook; // as in PInvLoader
     template <int BPT, int R, int STRIDE, int COLS, int THREADS>
     __device__ __forceinline__ void load_stage(float2 (&v)[BPT][R]) const
     {
@@ -186,6 +191,7 @@ struct PTLoader
             for (int r = 0; r < R; r++)
                 v[i][r] = __ldcg(p + (size_t)N2 * STRIDE * r);
         }
+        hook();
     }
 };
 
@@ -348,31 +354,65 @@ __device__ __forceinline__ void transform_dm_window(unsigned gi, unsigned B, uns
     }
 }
 
-// Thread 0 of a CTA: take the ticket it holds (fetching the next one, whose latency
-// overlaps the item), wait for the item's dependences, and return the verdict:
-// -1 stop (tickets exhausted; or, with stop_on_error, the launch failed), 0 skip
-// (outside the launch's transforms, or a failed wait), 1 run.
+// The completion count ticket t's item waits on and the value it needs: P1(f) waits
+// for slot f mod S to be released by P2(f - S), P2(f) for all P1(f).  False if t
+// holds no item of the launch's transforms.
 template <int n1t, int n2t>
-__device__ __forceinline__ int judge_ticket(const PersistArgs &a, long long total, unsigned &held, unsigned &t_out,
-                                            bool stop_on_error)
+__device__ __forceinline__ bool ticket_dependence(const PersistArgs &a, long long total, unsigned t,
+                                                  const unsigned *&cnt, unsigned &target)
 {
     constexpr int per_block = n1t + n2t;
-    const unsigned t = held;
-    t_out = t;
-    if ((long long)t >= total || (stop_on_error && *(volatile int *)a.err))
-        return -1;
-    held = atomicAdd(a.ticket, 1u);
+    if ((long long)t >= total)
+        return false;
     const long long q = t / per_block;
     const int w = (int)(t % per_block);
     const bool p1 = w < n1t;
     const long long f = p1 ? q : q - a.lag;
     if (f < 0 || f >= a.G)
-        return 0;
+        return false;
     const unsigned slot = (unsigned)f % (unsigned)a.S; // f < 2^31 (host check)
     const unsigned gen = (unsigned)f / (unsigned)a.S;
-    const bool ok = p1 ? wait_count(a.p2_done + slot, gen * n2t, a.err, a.timeout_ns)
-                       : wait_count(a.p1_done + slot, (gen + 1) * n1t, a.err, a.timeout_ns);
-    return ok ? 1 : 0;
+    cnt = p1 ? a.p2_done + slot : a.p1_done + slot;
+    target = p1 ? gen * n2t : (gen + 1) * n1t;
+    return true;
+}
+
+// Thread 0, during an item, once its loads are issued: look once (acquire load) at
+// the dependence of the next ticket it holds.  Returns that ticket if the dependence
+// is already met (counts only grow, so it stays met), else ~0u.  The acquire then
+// orders the next item's reads as judge_ticket's wait would, and the item boundary
+// skips that round trip.
+template <int n1t, int n2t>
+__device__ __forceinline__ unsigned ticket_precheck(const PersistArgs &a, long long total, unsigned t)
+{
+    const unsigned *cnt;
+    unsigned target;
+    if (!ticket_dependence<n1t, n2t>(a, total, t, cnt, target))
+        return ~0u;
+    return ld_acquire(cnt) >= target ? t : ~0u;
+}
+
+// Thread 0 of a CTA: take the ticket it holds (fetching the next one, whose latency
+// overlaps the item), wait for the item's dependences, and return the verdict:
+// -1 stop (tickets exhausted; or, with stop_on_error, the launch failed), 0 skip
+// (outside the launch's transforms, or a failed wait), 1 run.  ready_t: a ticket
+// whose dependence ticket_precheck() already saw met (no wait for it).
+template <int n1t, int n2t>
+__device__ __forceinline__ int judge_ticket(const PersistArgs &a, long long total, unsigned &held, unsigned &t_out,
+                                            bool stop_on_error, unsigned ready_t = ~0u)
+{
+    const unsigned t = held;
+    t_out = t;
+    if ((long long)t >= total || (stop_on_error && *(volatile int *)a.err))
+        return -1;
+    held = atomicAdd(a.ticket, 1u);
+    const unsigned *cnt;
+    unsigned target;
+    if (!ticket_dependence<n1t, n2t>(a, total, t, cnt, target))
+        return 0;
+    if (t == ready_t)
+        return 1;
+    return wait_count(cnt, target, a.err, a.timeout_ns) ? 1 : 0;
 }
 
 template <int N1, int N2, int MODE>
@@ -427,17 +467,25 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
 
     const long long total = (a.G + a.lag) * (long long)per_block;
     const int B = a.B;
-    unsigned held = 0; // thread 0: the ticket of the next item, fetched one item ahead
+    unsigned held = 0;    // thread 0: the ticket of the next item, fetched one item ahead
+    unsigned ready = ~0u; // thread 0: that ticket if its dependence was seen met during the item
     if (threadIdx.x == 0)
         held = atomicAdd(a.ticket, 1u);
+    // thread 0, once an item's first-stage loads are issued (the next ticket's atomic
+    // has returned by then): precheck the next item's dependence
+    auto precheck = [&]() {
+        if (threadIdx.x == 0)
+            ready = ticket_precheck<n1t, n2t>(a, total, held);
+    };
     for (unsigned it = 0;; it++)
     {
         const int par = it & 1;
         if (threadIdx.x == 0)
         {
             unsigned t;
-            s_verdict[par] = judge_ticket<n1t, n2t>(a, total, held, t, false);
+            s_verdict[par] = judge_ticket<n1t, n2t>(a, total, held, t, false, ready);
             s_ticket[par] = t;
+            ready = ~0u;
         }
         __syncthreads(); // also fences the previous item's shared-memory use
         const int verdict = s_verdict[par];
@@ -458,13 +506,16 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
         if (is_p1)
         {
             const int c0 = w * C1::COLS;
-            PInvLoader ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs, a.rbi + b};
+            PInvLoader<decltype(precheck)> ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs,
+                                              a.rbi + b, precheck};
             PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N2, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
             fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st, tw1L);
-            // publish: the barrier orders every thread's stores before thread 0's
-            // gpu-scope release reduction (release is cumulative) on the count
+            // publish: the barrier orders every thread's stores before one thread's
+            // gpu-scope release reduction (release is cumulative) on the count.  Warp 1
+            // publishes, so that its wait for the stores does not delay thread 0's
+            // next ticket.
             __syncthreads();
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 32)
                 asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p1_done + slot) : "memory");
         }
         else
@@ -482,8 +533,9 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             // first stage straight from the slot; its closing barrier means every
             // thread holds its inputs, so the slot may be refilled
             SmemIO<N1, C2::COLS> io{sm};
-            fft_stage<N1, C2::COLS, P_THREADS, +1, 1, false, true, true>(PTLoader{Ts, r0, N2}, io, tw2);
-            if (threadIdx.x == 0) // release: every thread's reads of the slot precede the count
+            fft_stage<N1, C2::COLS, P_THREADS, +1, 1, false, true, true>(
+                PTLoader<decltype(precheck)>{Ts, r0, N2, precheck}, io, tw2);
+            if (threadIdx.x == 32) // release: every thread's reads of the slot precede the count
                 asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p2_done + slot) : "memory");
             const size_t row = ((size_t)d * B + b) * M;
             PEpilogue<MODE, C2::COLS> ep{a.out_c64 ? a.out_c64 + row : nullptr,
