@@ -260,14 +260,14 @@ struct BinAcc
 // period, and phase is monotone within a run) is summed in registers and lands as
 // one shared atomic; other runs go sample by sample.  Zero samples are skipped as
 // foldDataPhase_kernel does.
-template <int COLS, int HALF>
+template <int COLS, int HALF, int THREADS = P_THREADS>
 __device__ __forceinline__ void fold_tile(const float *s_p, BinAcc *s_bins, uint64_t ph_b,
                                           uint64_t dphase, unsigned K, int r0, int N2)
 {
     constexpr int SAMPLES = COLS * HALF;
-    constexpr int PER_T = SAMPLES / P_THREADS;
+    constexpr int PER_T = SAMPLES / THREADS;
     constexpr int G = PER_T < COLS ? PER_T : COLS;
-    static_assert(SAMPLES % P_THREADS == 0 && PER_T % G == 0, "fold tile shape");
+    static_assert(SAMPLES % THREADS == 0 && PER_T % G == 0, "fold tile shape");
 #pragma unroll
     for (int g0 = 0; g0 < PER_T; g0 += G)
     {
@@ -316,11 +316,12 @@ __device__ __forceinline__ void fold_tile(const float *s_p, BinAcc *s_bins, uint
 // the CTA's consecutive pass-2 items of that trial and flushed to the global
 // double / u64 sums when the trial changes and at the end.  Each thread flushes and
 // clears the bins it owns; the callers' barriers order this against fold_tile().
+template <int THREADS = P_THREADS>
 __device__ __forceinline__ void fold_flush(BinAcc *s_bins, const FoldArgs &fa, int d, double scale2)
 {
     double *gs = fa.sum + (size_t)d * fa.K;
     unsigned long long *gc = fa.cnt + (size_t)d * fa.K;
-    for (unsigned i = threadIdx.x; i < fa.K; i += P_THREADS)
+    for (unsigned i = threadIdx.x; i < fa.K; i += THREADS)
     {
         const BinAcc v = s_bins[i];
         if (v.cnt)
@@ -415,8 +416,10 @@ __device__ __forceinline__ int judge_ticket(const PersistArgs &a, long long tota
     return wait_count(cnt, target, a.err, a.timeout_ns) ? 1 : 0;
 }
 
-template <int N1, int N2, int MODE>
-__global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArgs a)
+// THREADS x 2 CTAs per SM; BIG: radix-16/32 register stages (32 values per thread at
+// 256 threads), else radix-8 stages (16 values per thread at 512 threads).
+template <int N1, int N2, int MODE, int THREADS, bool BIG>
+__global__ void __launch_bounds__(THREADS, 2) inv_persistent_kernel(PersistArgs a)
 {
     using C1 = PCfg<N2>; // pass 1: columns of length N2
     using C2 = PCfg<N1>; // pass 2: rows of length N1
@@ -426,11 +429,11 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     constexpr int per_block = n1t + n2t;
     constexpr int F = N1 * N2;
     constexpr int M = F / 2;
-    constexpr int NSL = LastNs<N2, 1, true>::value;     // pass 1, last stage: Ns
-    constexpr int R2F = StageRadix<N1, 1, true>::value; // pass 2, first stage: radix
+    constexpr int NSL = LastNs<N2, 1, BIG>::value;     // pass 1, last stage: Ns
+    constexpr int R2F = StageRadix<N1, 1, BIG>::value; // pass 2, first stage: radix
     // two-stage pass 1 (radix R1F then the last stage): its only stage twiddles are
     // the last stage's, so the [r][k] table replaces the W_{N2} table
-    constexpr bool P1_TWO = NSL == StageRadix<N2, 1, true>::value;
+    constexpr bool P1_TWO = NSL == StageRadix<N2, 1, BIG>::value;
     constexpr bool FOLD = (MODE & OUT_FOLD) != 0;
     // fold-only bins hold unscaled |x|^2: 1/F^2 at the flush (exact, F a power of two)
     constexpr double FLUSH_SCALE2 = (MODE == OUT_FOLD) ? 1.0 / ((double)F * (double)F) : 1.0;
@@ -449,18 +452,18 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     __shared__ unsigned s_ticket[2];
     __shared__ int s_verdict[2];
 
-    for (int i = threadIdx.x; i < N2; i += P_THREADS)
+    for (int i = threadIdx.x; i < N2; i += THREADS)
     {
         const int r = i / NSL, k = i % NSL; // r*k < N2
         tw1L[i] = __ldg(a.tw.twN2 + r * k);
         if constexpr (!P1_TWO)
             tw1[i] = __ldg(a.tw.twN2 + i);
     }
-    for (int i = threadIdx.x; i < N1; i += P_THREADS)
+    for (int i = threadIdx.x; i < N1; i += THREADS)
         tw2[i] = __ldg(a.tw.twN1 + i);
     if constexpr (FOLD)
     {
-        for (unsigned i = threadIdx.x; i < a.fold.K; i += P_THREADS)
+        for (unsigned i = threadIdx.x; i < a.fold.K; i += THREADS)
             s_bins[i] = BinAcc{0.0f, 0u};
     }
     int fold_d = -1; // the DM trial s_bins holds (uniform over the CTA)
@@ -509,7 +512,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
             PInvLoader<decltype(precheck)> ld{a.ring, a.H + (size_t)d * F, a.delays + (size_t)d * F, c0, N1, F, a.fbs,
                                               a.rbi + b, precheck};
             PStoreT st{Ts, a.tw.lo, a.tw.hi, c0, N2, (unsigned)(N2 - 1), __builtin_ctz((unsigned)N2)};
-            fft_stages<N2, C1::COLS, P_THREADS, +1, 1, true, true>(sm, tw1, ld, st, tw1L);
+            fft_stages<N2, C1::COLS, THREADS, +1, 1, true, BIG>(sm, tw1, ld, st, tw1L);
             // publish: the barrier orders every thread's stores before one thread's
             // gpu-scope release reduction (release is cumulative) on the count.  Warp 1
             // publishes, so that its wait for the stores does not delay thread 0's
@@ -526,14 +529,14 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                 if (d != fold_d)
                 {
                     if (fold_d >= 0)
-                        fold_flush(s_bins, a.fold, fold_d, FLUSH_SCALE2);
+                        fold_flush<THREADS>(s_bins, a.fold, fold_d, FLUSH_SCALE2);
                     fold_d = d;
                 }
             }
             // first stage straight from the slot; its closing barrier means every
             // thread holds its inputs, so the slot may be refilled
             SmemIO<N1, C2::COLS> io{sm};
-            fft_stage<N1, C2::COLS, P_THREADS, +1, 1, false, true, true>(
+            fft_stage<N1, C2::COLS, THREADS, +1, 1, false, true, BIG>(
                 PTLoader<decltype(precheck)>{Ts, r0, N2, precheck}, io, tw2);
             if (threadIdx.x == 32) // release: every thread's reads of the slot precede the count
                 asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.p2_done + slot) : "memory");
@@ -547,10 +550,10 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
                                          N1,
                                          N2,
                                          1.0f / (float)F};
-            fft_stages<N1, C2::COLS, P_THREADS, +1, R2F, false, true, FOLD>(sm, tw2, PNoLoad{}, ep);
+            fft_stages<N1, C2::COLS, THREADS, +1, R2F, false, BIG, FOLD>(sm, tw2, PNoLoad{}, ep);
             if constexpr (FOLD)
             {
-                fold_tile<C2::COLS, N1 / 2>(s_p, s_bins,
+                fold_tile<C2::COLS, N1 / 2, THREADS>(s_p, s_bins,
                                             fold_phase0(a.fold) + (uint64_t)((uint64_t)b * (uint64_t)M) * a.fold.dphase,
                                             a.fold.dphase, a.fold.K, r0, N2);
                 // s_p and the bins are next touched after the next ticket barrier
@@ -560,7 +563,7 @@ __global__ void __launch_bounds__(P_THREADS, 2) inv_persistent_kernel(PersistArg
     if constexpr (FOLD)
     {
         if (fold_d >= 0)
-            fold_flush(s_bins, a.fold, fold_d, FLUSH_SCALE2);
+            fold_flush<THREADS>(s_bins, a.fold, fold_d, FLUSH_SCALE2);
     }
 }
 
@@ -944,24 +947,24 @@ void ensure_l2_persisting(size_t bytes)
 // carveout_blocks > 0: ask for a shared-memory carveout that holds that many CTAs
 // (the occupancy query and the launch otherwise assume a smaller default split).
 template <class KERNEL, class... EXTRA>
-cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kMaxDevices], int per_block,
-                                     int max_per_sm, int carveout_blocks, int F, const PersistArgs &a, int sms,
-                                     cudaStream_t st, PersistPlan *plan, EXTRA... extra)
+cudaError_t launch_persistent_kernel(KERNEL k, int threads, size_t smem, size_t (&granted)[kMaxDevices],
+                                     int per_block, int max_per_sm, int carveout_blocks, int F, const PersistArgs &a,
+                                     int sms, cudaStream_t st, PersistPlan *plan, EXTRA... extra)
 {
     cudaError_t e = ensure_smem(k, smem, granted);
     if (e != cudaSuccess)
     {
-        set_launch_failure_detail("persistent inverse transform", "shared-memory attribute", 0, 0, P_THREADS, smem);
+        set_launch_failure_detail("persistent inverse transform", "shared-memory attribute", 0, 0, threads, smem);
         return e;
     }
     if (carveout_blocks > 0 && (e = prefer_carveout(k, smem, carveout_blocks)) != cudaSuccess)
     {
         (void)cudaGetLastError();
-        set_launch_failure_detail("persistent inverse transform", "carveout attribute", 0, 0, P_THREADS, smem);
+        set_launch_failure_detail("persistent inverse transform", "carveout attribute", 0, 0, threads, smem);
         return e;
     }
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P_THREADS, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
     if (e != cudaSuccess)
         return e;
     const int occupancy = per_sm;
@@ -999,7 +1002,7 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
     ensure_l2_persisting(slot_bytes);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(P_THREADS);
+    cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     // the window cannot exceed the device's maximum access-policy window (the largest
@@ -1027,23 +1030,34 @@ cudaError_t launch_persistent_kernel(KERNEL k, size_t smem, size_t (&granted)[kM
     if (e == cudaSuccess)
         e = cudaGetLastError();
     if (e != cudaSuccess)
-        set_launch_failure_detail("persistent inverse transform", "launch", grid, 1, P_THREADS, smem);
+        set_launch_failure_detail("persistent inverse transform", "launch", grid, 1, threads, smem);
     return e;
 }
+
+// Register plan of the FP32 persistent transform for F = N1 x N2: 256 threads with
+// radix-16/32 stages, or 512 threads with radix-8 stages.
+template <int N1, int N2>
+struct PersistPlanOf
+{
+    static constexpr int THREADS = P_THREADS;
+    static constexpr bool BIG = true;
+};
 
 template <int N1, int N2, int MODE>
 cudaError_t persist_launch(const PersistArgs &a, int sms, cudaStream_t st, PersistPlan *plan)
 {
     using C1 = PCfg<N2>;
     using C2 = PCfg<N1>;
+    constexpr int THREADS = PersistPlanOf<N1, N2>::THREADS;
+    constexpr bool BIG = PersistPlanOf<N1, N2>::BIG;
     constexpr int DATA = (C1::SMEM_DATA > C2::SMEM_DATA) ? C1::SMEM_DATA : C2::SMEM_DATA;
-    constexpr bool P1_TWO = LastNs<N2, 1, true>::value == StageRadix<N2, 1, true>::value;
+    constexpr bool P1_TWO = LastNs<N2, 1, BIG>::value == StageRadix<N2, 1, BIG>::value;
     const size_t smem = (size_t)(DATA + N1 + (P1_TWO ? N2 : 2 * N2)) * sizeof(float2) +
                         (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
     static size_t granted[kMaxDevices] = {};
     constexpr int per_block = N1 / C1::COLS + N2 / C2::COLS;
-    return launch_persistent_kernel(inv_persistent_kernel<N1, N2, MODE>, smem, granted, per_block, 1 << 20, 0,
-                                    N1 * N2, a, sms, st, plan);
+    return launch_persistent_kernel(inv_persistent_kernel<N1, N2, MODE, THREADS, BIG>, THREADS, smem, granted,
+                                    per_block, 1 << 20, 0, N1 * N2, a, sms, st, plan);
 }
 
 template <int MODE, bool BF16>
@@ -1052,7 +1066,7 @@ cudaError_t tc_launch(const PersistArgs &a, const TcArgs &tc, int sms, cudaStrea
     const size_t smem = 1024 + TC_BINS + (((MODE & OUT_FOLD) != 0) ? (size_t)a.fold.K * 8 : 0);
     static size_t granted[kMaxDevices] = {};
     // at most 512 / 128 CTAs per SM can hold their tensor-memory columns at once
-    return launch_persistent_kernel(inv_tc_kernel<MODE, BF16>, smem, granted, 2 * (TC_N / TC_COLS),
+    return launch_persistent_kernel(inv_tc_kernel<MODE, BF16>, P_THREADS, smem, granted, 2 * (TC_N / TC_COLS),
                                     512 / (int)TC_TMEM_COLS, 2, TC_N * TC_N, a, sms, st, plan, tc);
 }
 
