@@ -495,7 +495,10 @@ def run_two_pol(args, w, rank, world, local):
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": bytes_per_launch / (per_launch_ms * 1e-3) / 1e9, "peak": peak,
         "unit": "GB/s", "frac": bytes_per_launch / (per_launch_ms * 1e-3) / 1e9 / peak, "peak_source": f"of {peak_src}",
-        "traffic": None, "bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms,
+        "traffic": (tr * trans) if (tr := profile_traffic("inv_persistent_two_pol")) is not None else None,
+        "traffic_note": "ncu DRAM bytes of the second polarisation's (fused-fold) launch per transform, "
+                        "scaled to this launch's transforms",
+        "bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms,
         "pipeline_achieved": BYTES_PER_UNIT * units_rank * args.steps / (t_ms * 1e-3) / 1e9,
     }
     # end to end from pinned host memory, one pass over both polarisations per step
