@@ -36,3 +36,23 @@ def test_int8_baseband_is_clipped_gaussian_and_seeded():
     assert x.min() >= -127 and x.max() <= 127
     assert abs(float(np.std(x.astype(np.float64))) - 20.0) < 0.5
     np.testing.assert_array_equal(x, bench.int8_baseband(1 << 16, 20.0, 7))
+
+
+def test_workload_config_is_the_same_object_for_both_arms():
+    """Both arms print workload_config(); its sizes follow the workload, and only the
+    workloads whose step fits in L2 are timed with L2 overwritten between steps."""
+    import types
+
+    for name, w in bench.WORKLOADS.items():
+        if "n_sources" in w:
+            continue
+        args = types.SimpleNamespace(workload=name, precision="fp32")
+        c = bench.workload_config(args, dict(w), 2)
+        assert c == bench.workload_config(args, dict(w), 2)
+        assert c["workload"] == name and c["fft_size"] == w["fftpoint"] and c["M"] == w["fftpoint"] // 2
+        assert c["dm_trials_per_gpu"] == w["n_dms"] and c["batch"] == w["batch"]
+        assert c["parallelism"] == "dm-shard x2"
+        assert ("L2 flushed" in c["l2"]) == bench.fits_in_l2(w)
+    assert not bench.fits_in_l2(bench.WORKLOADS["many_dm_512"])
+    assert not bench.fits_in_l2(bench.WORKLOADS["two_pol_1024"])
+    assert bench.fits_in_l2(bench.WORKLOADS["single_dm_50"])
