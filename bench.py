@@ -61,11 +61,11 @@ WORKLOADS = {
     "single_dm_50": dict(bw=16e6, centre=1400e6, n_dms=1, dm_lo=50.0, dm_hi=50.0, fftpoint=1 << 16, batch=32,
                          nbins=256, samples=1 << 22, period=0.033, inject_dm=50.0, snr_db=-10.0, duty=0.05),
     # 2-pol int8 I/Q (Gaussian, sigma 20, clipped), 1024 DMs log-uniform in 1..1000 (seed 4,
-    # sorted), which forces F = 2^20; the fused 2-pol fold (msosm_attach_fold_pol2); 16 windows
-    # per call (2 / 4 / 8 / 16 measured 6.13 / 6.19 / 6.29 / 6.36e10 on 256 DMs: fewer response
-    # re-reads)
+    # sorted), which forces F = 2^20; the fused 2-pol fold (msosm_attach_fold_pol2); 8 windows
+    # per call (2 / 4 / 8 / 16 measured 6.13 / 6.19 / 6.29 / 6.36e10 on 256 DMs, fewer response
+    # re-reads; at full size 8 gave 6.39e10 and 16 6.31e10)
     "two_pol_1024": dict(bw=128e6, centre=820e6, n_dms=1024, dm_lo=1.0, dm_hi=1000.0, dm_dist="loguniform",
-                         fftpoint=1 << 20, batch=16, nbins=256, samples=1 << 28, period=0.0071, pols=2, sigma=20.0),
+                         fftpoint=1 << 20, batch=8, nbins=256, samples=1 << 28, period=0.0071, pols=2, sigma=20.0),
     # DM refinement: 64 simulated sources of 2^20..2^24 samples (log-uniform, seed 5), true
     # DMs uniform in 10..300, guesses 0.5 DM off, 20 steps each on the smoothed sharpness
     # (pymsosm.refine); 16 MHz at 1400 MHz, 2 ms period, 2 % Gaussian pulse, -10 dB
