@@ -921,9 +921,10 @@ static int process_one(msosm_t *h, const void *in, bool in_on_device, cudaStream
         pa.timeout_ns = kWaitTimeoutNs;
         pa.max_ctas_per_sm = h->ctas_per_sm;
         pa.D = h->D;
-        // default order: window-major groups of 8 DM trials up to 2^18-point transforms
-        // (+0.9 % on the 512-DM, 2^18 workload), DM-major above (groups cost 2.5 % at 2^20)
-        const int dm_group = h->dm_group > 0 ? h->dm_group : (h->g.L <= 18 ? 8 : 1);
+        // default order: window-major groups of 4 DM trials up to 2^18-point transforms
+        // (512-DM, 2^18 workload: groups of 1 / 2 / 3 / 4 / 8 / 16 / 32 measured 9.42 / 9.59 /
+        // 9.63 / 9.64 / 9.51 / 9.32 / 9.29e10), DM-major above (groups cost 2.5 % at 2^20)
+        const int dm_group = h->dm_group > 0 ? h->dm_group : (h->g.L <= 18 ? 4 : 1);
         pa.dm_group = std::max(1, std::min(dm_group, h->D));
         msosm::TcArgs tc{static_cast<const uint4 *>(h->d_tc_op), h->d_absmax, h->hmax};
         const bool use_tc = h->precision != msosm::PREC_FP32;

@@ -211,7 +211,7 @@ int msosm_autotune(float bw, float f0, const float *dms, int num_dms, int batch,
  * flight, less L2 pressure at large F), and the transform order: DM trials in groups of
  * dm_group, window-major inside a group, so that consecutive transforms gather from
  * nearly the same spectra-ring lines (0 keeps the current order; 1 = DM-major; until set,
- * groups of 8 for transforms of up to 2^18 points and DM-major above).  Series outputs do
+ * groups of 4 for transforms of up to 2^18 points and DM-major above).  Series outputs do
  * not depend on either; fused folds only to the order of their float sums.  No counterpart
  * in the reference. */
 int msosm_set_launch_shape(msosm_t *h, int ctas_per_sm, int dm_group);
